@@ -1,0 +1,303 @@
+#!/usr/bin/env python3
+"""Benchmark: rays/s of the Monte Carlo view-factor tracer on one GB300.
+
+Workload: the 64-surface mixed scene from seed 2 (16 cylinders, 16 frusta,
+12 discs, 10 annuli, 10 spheres; radii U[0.05,1], lengths U[0.1,2], random
+axes, centres U[-3,3]^3), 1e8 rays per step spread over the emitters by area.
+A step is one pass of the tracer over those 1e8 rays.
+
+* value   -- rays/s of the timed kernel path with the scene resident on the
+             device (CUDA events on the library's stream around each step).
+* e2e     -- the same through the C ABI with host buffers: scene upload,
+             trace, FP64 normalisation and read-back of the tallies and F.
+* roofline -- FP32 issue roofline of the tracing kernel: algorithmic FP32
+             operations per ray (per-type costs, FMA = 1) / kernel time,
+             against the device's measured dependent-FMA issue rate.
+* cpu_baseline -- the CPU restatement of the reference kernel on all host
+             cores over a bounded sample of the same workload.
+
+``--impl reference`` times that CPU restatement alone on the same workload
+(the reference's OpenCL kernel cannot run without an OpenCL runtime).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+# FP32 operations per call from the source of RayFactorGPU.cl (FMA/mad = 1, MUFU not counted).
+TEST_OPS = {0: 33, 1: 39, 2: 33, 3: 23, 4: 21, 5: 23}      # per ray x surface test, by type
+EMIT_OPS = {0: 52, 1: 58, 2: 55, 3: 52, 4: 48, 5: 50}      # per emitted ray, by emitter type
+METRIC = "rays/s on 1 GB300: batched mixed-precision vs plain kernel at equal F error"
+
+
+def algorithmic_ops(scene, rays) -> float:
+    types = scene.primitives["type"].astype(int)
+    per_ray_tests = float(sum(TEST_OPS[t] for t in types))
+    return float(sum(int(r) * (EMIT_OPS[int(t)] + per_ray_tests) for r, t in zip(rays, types)))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.rows = []
+        self.proc = None
+        self.device = device
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[4 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args):
+    from rayfactorcl_gb300 import generators
+    return generators.mixed_scene(seed=2, total_rays=args.rays)
+
+
+def cpu_rate(w, seconds: float, threads: int = 0):
+    """Oracle rays/s on host cores over a bounded, area-weighted sample."""
+    from oracle import oracle as O
+    p = O.params(compat=0, key1=w.key1)
+    probe = np.maximum((w.rays // 20000) // 4 * 4, 4)
+    t0 = time.perf_counter()
+    O.tally(w.scene, p, probe, threads=threads)
+    dt = time.perf_counter() - t0
+    scale = max(1.0, seconds / max(dt, 1e-3))
+    sample = np.maximum((probe * scale).astype(np.int64) // 4 * 4, 4)
+    t0 = time.perf_counter()
+    O.tally(w.scene, p, sample, threads=threads)
+    dt = time.perf_counter() - t0
+    nthreads = threads if threads > 0 else O.max_threads()
+    return float(sample.sum()) / dt, int(sample.sum()), nthreads, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    w = workload(args)
+    from oracle import oracle as O
+    O.lib()
+    rates = []
+    sample_rays = 0
+    for i in range(args.warmup + args.steps):
+        rate, sample_rays, nthreads, _ = cpu_rate(w, seconds=args.ref_seconds)
+        if i >= args.warmup:
+            rates.append(rate)
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.rays / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": "mixed64 seed 2, 64 surfaces, 1e8 rays/step",
+                                        "kernel": "CPU restatement of RayFactorGPU.cl runGPU"},
+        "cpu_baseline": {"value": value, "unit": "rays/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{sample_rays} rays of the workload per step, area-weighted"},
+        "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    from rayfactorcl_gb300 import _lib
+    from rayfactorcl_gb300.tracer import PREC_EXACT, PREC_FAST, Tracer
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    _lib.load()
+    w = workload(args)
+    sc = w.scene
+    rays = w.rays
+    total_rays = int(rays.sum())
+    ops = algorithmic_ops(sc, rays)
+    prec = {"exact": PREC_EXACT, "fast": PREC_FAST}[args.precision]
+
+    fma = __import__("ctypes").c_double()
+    _lib.check(_lib.load().rf_measure_fp32_peak(local, fma))
+    peak_ops = fma.value
+
+    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # -- value: scene resident, per-step device time ----------------------
+    t = Tracer(precision=prec, key1=w.key1, device=local)
+    t.set_scene(sc)
+    stream = torch.cuda.ExternalStream(t.stream_handle, device=f"cuda:{local}")
+    for _ in range(args.warmup):
+        t.trace_async(rays)
+        torch.cuda.synchronize()
+    step_ms, kern_ms = [], []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                l2_flush.zero_()  # inputs are smaller than L2: flush it between steps
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            t.trace_async(rays)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            kern_ms.append(t.last_stats()[0])
+        torch.cuda.synchronize()
+    barrier()
+    hits = np.zeros((sc.n, sc.n), np.uint64)
+    t.read_results(hits, None)
+    assert int(hits.sum()) <= total_rays
+    ms_step = float(np.mean(step_ms))
+    if world > 1:
+        import torch.distributed as dist
+        m = torch.tensor([ms_step], device=f"cuda:{local}")
+        dist.all_reduce(m, op=dist.ReduceOp.MAX)
+        ms_step = float(m.item())
+    value = world * total_rays / (ms_step * 1e-3)
+    kernel_ms = float(np.mean(kern_ms))
+    achieved = ops / (kernel_ms * 1e-3)
+
+    # -- e2e: host buffers through the C ABI ----------------------------
+    F = np.zeros((sc.n, sc.n), np.float64)
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t.set_scene(sc)
+        h2, F2 = t.trace(rays)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = e2e_ms[args.warmup:]
+    h2d = sc.primitives.nbytes + sc.n * 64 + rays.nbytes + 32 * sc.n + 8 * sc.n
+    d2h = sc.n * sc.n * 16
+    t.close()
+
+    # -- CPU baseline -----------------------------------------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, sample_rays, nthreads, dt = cpu_rate(w, seconds=args.cpu_seconds)
+        cpu = {"value": rate, "unit": "rays/s", "cores": nthreads, "kind": "port",
+               "sample": f"{sample_rays} rays of the workload, area-weighted, {dt:.1f} s"}
+
+    traffic = None
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get(f"{args.precision}_plain_bytes_per_launch")
+        except (ValueError, OSError):
+            traffic = None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "mixed64 seed 2: 64 surfaces (16 cyl, 16 frustum, 12 disc, 10 annulus, "
+                               "10 sphere), 1e8 rays/step spread by area",
+                   "kernel": f"plain ({args.precision})", "l2": "flushed between steps (256 MB write)",
+                   "rays_per_step": total_rays},
+        "e2e": {"value": world * total_rays / (float(np.mean(e2e_ms)) * 1e-3), "unit": "rays/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp32-issue", "achieved": achieved / 1e12, "peak": peak_ops / 1e12,
+                     "unit": "Top/s (FP32, FMA = 1 op)", "frac": achieved / peak_ops,
+                     "traffic": traffic,
+                     "peak_source": "measured in-run: dependent-FMA issue probe (rf_measure_fp32_peak)"},
+        "kernel_ms": kernel_ms,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="exact", choices=["exact", "fast"])
+    ap.add_argument("--rays", type=int, default=100_000_000)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,212 @@
+/*
+ * rayfactor_gb300.h -- C ABI of the GB300 (sm_103a) Monte Carlo view-factor
+ * tracer.  Drop-in for the tracing path of RayFactorCL: the OpenCL kernels
+ * runGPU / runBVGPU (RayFactorCL/RayFactorGPU.cl:481-626) and the launch,
+ * tally and normalisation logic of runCL_GPURNG (RayFactorCL/main.cpp:54-272).
+ *
+ * Plain C types only.  The scene tables are the reference's own structs
+ * (RayFactorCL/RayfactorConstants.h:38-56) byte for byte, so a caller holding
+ * a reference Scene passes &scene.primitives[0] and &scene.boundingVolumes[0]
+ * unchanged.  Every function returns an rf_status; none exits the process.
+ * One rf_ctx per host thread: calls on one context are not re-entrant, but
+ * several contexts may share a GPU.
+ */
+#ifndef RAYFACTOR_GB300_H
+#define RAYFACTOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RF_ABI_VERSION 1
+
+/* Error codes (replace CHECK/CHECKERR -> exit(1), RayFactorCL/util_opencl.h:123-131). */
+typedef enum rf_status {
+    RF_OK = 0,
+    RF_ERR_INVALID_ARG = 1,  /* null pointer, negative size, bad enum               */
+    RF_ERR_BAD_SCENE = 2,    /* unknown type, non-finite transform, bad BV range    */
+    RF_ERR_OOM = 3,          /* device or host allocation failed                    */
+    RF_ERR_CUDA = 4,         /* a CUDA runtime call failed (see rf_last_error)      */
+    RF_ERR_TIMEOUT = 5,      /* a bounded device wait gave up                       */
+    RF_ERR_OVERFLOW = 6,     /* a ray budget or launch size does not fit            */
+    RF_ERR_NO_DEVICE = 7,    /* no CUDA device / device index out of range          */
+    RF_ERR_UNSUPPORTED = 8,  /* mode not available for this scene or device         */
+    RF_ERR_STATE = 9         /* call order (e.g. rf_trace before rf_set_scene)      */
+} rf_status;
+
+/* RayfactorConstants.h:25-33 */
+typedef enum rf_primitive_type {
+    RF_CYLINDER = 0, RF_FRUSTUM = 1, RF_SPHERE = 2, RF_ANNULUS = 3,
+    RF_RECTANGLE = 4, RF_DISC = 5, RF_NONE = 6
+} rf_primitive_type;
+
+/* RayfactorConstants.h:38-45 -- 112 bytes.  m / invm: row-major 3x4
+ * object->world and world->object transforms; util1: frustum top radius or
+ * annulus inner radius^2; util2: annulus outer radius^2 or the inward/outward
+ * normal sign (-1/+1) of cylinders, frusta and spheres. */
+typedef struct rf_primitive {
+    float m[12];
+    float invm[12];
+    int32_t type;
+    int32_t rayDensity;
+    float util1;
+    float util2;
+} rf_primitive;
+
+/* RayfactorConstants.h:48-56 -- 72 bytes.  Children are primitives
+ * [objStartIndex, objEndIndex); settings == 1 tests them immediately. */
+typedef struct rf_bounding_volume {
+    float invm[12];
+    int32_t type;
+    int32_t settings;
+    int32_t objStartIndex;
+    int32_t objEndIndex;
+    float util1;
+    float util2;
+} rf_bounding_volume;
+
+/* Behaviour of the reference that is kept only on request.  RF_COMPAT_ALL
+ * reproduces the reference run for run; the default (0) fixes each item. */
+#define RF_COMPAT_BUDGET   (1u << 0) /* every emitter gets emitter 0's budget (main.cpp:172)  */
+#define RF_COMPAT_SPHERE   (1u << 1) /* sphere discriminant without sqrt (RayFactorGPU.cl:272) */
+#define RF_COMPAT_BV_STALE (1u << 2) /* stale child index across BVs (RayFactorGPU.cl:596-619) */
+#define RF_COMPAT_STREAMS  (1u << 3) /* stream key {gid, key1} only: all emitters share streams
+                                        (RayFactorGPU.cl:486-487)                              */
+#define RF_COMPAT_ALL      (RF_COMPAT_BUDGET | RF_COMPAT_SPHERE | RF_COMPAT_BV_STALE | RF_COMPAT_STREAMS)
+
+/* Arithmetic of the intersection code. */
+typedef enum rf_precision {
+    RF_PREC_EXACT = 0, /* IEEE FP32 with the fixed op mapping: per-ray bit-exact with the
+                          CPU restatement of RayFactorGPU.cl (the "plain" kernel)           */
+    RF_PREC_FAST = 1,  /* FP32 with hardware approximations, like OpenCL native_*           */
+    RF_PREC_MIXED = 2, /* batched kernel: FP32 approximations, quadric roots that fail a
+                          conditioning test recomputed in FP64                              */
+    RF_PREC_FP64 = 3   /* FP64 throughout on identical streams: the FP64 tracer             */
+} rf_precision;
+
+typedef struct rf_config {
+    uint32_t struct_size; /* sizeof(rf_config); set by rf_config_default                    */
+    uint32_t compat;      /* RF_COMPAT_* bits                                               */
+    uint32_t precision;   /* rf_precision                                                   */
+    uint32_t key1;        /* Philox key word 1 (0xdecafbad in RayFactorGPU.cl:486)           */
+    float eps;            /* self-hit threshold on t (1e-3f, RayFactorGPU.cl:7)              */
+    int32_t device;       /* CUDA device ordinal                                            */
+    int32_t block_size;   /* 0: autotuned / built-in default                                */
+    int32_t rays_per_thread; /* 0: default; 4 or 8 (one or two Philox draws)                */
+    uint32_t scene_id;    /* folded into the stream counter outside RF_COMPAT_STREAMS       */
+    uint32_t reserved[7];
+} rf_config;
+
+typedef struct rf_ctx rf_ctx;
+
+/* Reference-compatible defaults: compat = 0, EXACT, key1 = 0xdecafbad, eps = 1e-3. */
+void rf_config_default(rf_config *cfg);
+
+rf_status rf_create(rf_ctx **ctx, const rf_config *cfg);
+void rf_destroy(rf_ctx *ctx);
+const char *rf_last_error(const rf_ctx *ctx);
+const char *rf_status_string(rf_status s);
+int32_t rf_abi_version(void);
+
+/* Copy a scene to the device (replaces the clCreateBuffer/clEnqueueWriteBuffer of
+ * main.cpp:113-149).  The caller keeps ownership of both tables. */
+rf_status rf_set_scene(rf_ctx *ctx, const rf_primitive *prims, int32_t n_prims,
+                       const rf_bounding_volume *bvs, int32_t n_bvs);
+
+/* Trace rays_per_emitter[e] rays from every emitter e (0 = skip) and tally the
+ * first surface hit (RayFactorGPU.cl:481-626, one launch for all emitters
+ * instead of main.cpp:168-181's launch per emitter).  use_bv selects runBVGPU
+ * semantics.  hits_out: n x n int64 tallies, row = emitter (caller-owned, may be
+ * NULL); F_out: n x n doubles hits/rays (main.cpp:241-249, FP64; NaN for rows
+ * with no rays; may be NULL).  Synchronous. */
+rf_status rf_trace(rf_ctx *ctx, const int64_t *rays_per_emitter, int32_t use_bv,
+                   uint64_t *hits_out, double *F_out);
+
+/* The same, split for callers that time or overlap the GPU work:
+ * rf_trace_async enqueues on the context's stream and returns; rf_read_results
+ * waits and copies the tallies (and F) of the last trace. */
+rf_status rf_trace_async(rf_ctx *ctx, const int64_t *rays_per_emitter, int32_t use_bv);
+rf_status rf_read_results(rf_ctx *ctx, uint64_t *hits_out, double *F_out);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that record their
+ * own events or order other work after a trace. */
+void *rf_stream(rf_ctx *ctx);
+
+/* Milliseconds of the last trace's kernels on the device (CUDA events on the
+ * context's stream) and the number of kernel launches it made. */
+rf_status rf_last_trace_stats(rf_ctx *ctx, double *kernel_ms, int32_t *launches);
+
+/* Per-ray first-hit index (-1 = none) of rays [first_ray, first_ray+n_rays) of
+ * one emitter, for parity checks against the CPU restatement. */
+rf_status rf_trace_rays(rf_ctx *ctx, int32_t emitter, int64_t first_ray, int64_t n_rays,
+                        int32_t use_bv, int32_t *hit_index_out);
+
+/* runCL_GPURNG (main.cpp:54-272) without the file output: budget per emitter
+ * = round_to_128(rayDensity * n_samples / 4) * 4 (main.cpp:172-173;
+ * RF_COMPAT_BUDGET uses emitter 0's rayDensity for all), kernel chosen by
+ * use_bv (main.cpp:68-75), tallies normalised by the rays shot (main.cpp:178,
+ * 241-249).  rays_out (n, may be NULL) receives the budgets. */
+rf_status rf_run_gpurng(rf_ctx *ctx, int32_t n_samples, int32_t use_bv, int64_t *rays_out,
+                        uint64_t *hits_out, double *F_out);
+
+/* The budget rule alone (host arithmetic, no GPU). */
+rf_status rf_ray_budgets(const rf_primitive *prims, int32_t n_prims, int32_t n_samples,
+                         uint32_t compat, int64_t *rays_out);
+
+/* Write F like main.cpp:236-249: one row per emitter, 8 significant digits,
+ * every value followed by a comma. */
+rf_status rf_write_output_txt(const char *path, const double *F, int32_t n);
+
+/* ---------------------------------------------------------------------------
+ * Batched mixed-precision tracing: many independent scenes, many emitters with
+ * uneven budgets, one persistent launch that pulls (scene, emitter, ray chunk)
+ * work items from a device queue.
+ * ------------------------------------------------------------------------- */
+typedef struct rf_scene_desc {
+    const rf_primitive *prims;
+    int32_t n_prims;
+    int32_t reserved;
+    const int64_t *rays_per_emitter; /* initial budget per emitter (n_prims entries) */
+} rf_scene_desc;
+
+/* Trace every scene once with its budgets.  hits_out: the scenes' n_i x n_i
+ * tally matrices back to back (sum n_i^2 entries); F_out likewise (may be NULL). */
+rf_status rf_trace_batch(rf_ctx *ctx, const rf_scene_desc *scenes, int32_t n_scenes,
+                         uint64_t *hits_out, double *F_out);
+
+/* Convergence loop: add rays to every emitter whose row still has a binomial
+ * standard error sqrt(F(1-F)/rays) above tol, in rounds of round_rays per
+ * emitter, until every row is below tol or max_rounds rounds ran.  The round is
+ * a CUDA graph (trace + FP64 normalisation + convergence test) replayed by a
+ * device-side loop.  rays_out (sum n_i, may be NULL) gets the final budgets;
+ * rounds_out the rounds run. */
+rf_status rf_converge_batch(rf_ctx *ctx, const rf_scene_desc *scenes, int32_t n_scenes,
+                            double tol, int64_t round_rays, int32_t max_rounds,
+                            uint64_t *hits_out, double *F_out, int64_t *rays_out,
+                            int32_t *rounds_out);
+
+/* FP64 checks on a tally (device, FP64): max |sum_j F_ij - 1| over rows
+ * (summation rule of a closed enclosure) and max |A_i F_ij - A_j F_ji| /
+ * max(A_i F_ij, A_j F_ji) over pairs with both tallies non-zero (reciprocity). */
+rf_status rf_check_F(rf_ctx *ctx, const double *F, const double *areas, int32_t n,
+                     double *max_sum_err, double *max_recip_err);
+
+/* Pick block size, rays per thread and tallying for the current scene by
+ * timing short runs; the choice is cached per scene shape in memory and, when
+ * cache_path is not NULL, in that file.  Applies the choice to the context. */
+rf_status rf_autotune(rf_ctx *ctx, int32_t use_bv, const char *cache_path);
+
+/* Counters of the last mixed-precision run: tests re-evaluated in FP64. */
+rf_status rf_last_refine_count(rf_ctx *ctx, uint64_t *refined_tests);
+
+/* FP32 issue-rate probe: dependent-FMA throughput of the device in FMA/s
+ * (one FMA counted as one operation), measured with CUDA events. */
+rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,669 @@
+// rf_capi.cu -- the C ABI (include/rayfactor_gb300.h): contexts, scene
+// validation and upload, launch planning, tallies, normalisation and output.
+//
+// Replaces runCL_GPURNG (RayFactorCL/main.cpp:54-272) and the OpenCL device
+// layer (RayFactorCL/util_opencl.h:133-352) with the CUDA runtime on one GPU.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "rayfactor_gb300.h"
+#include "rf_internal.h"
+
+using namespace rf;
+
+namespace {
+
+constexpr int32_t kMaxPrims = 16384;            // n x n int64 tallies: 2 GiB
+constexpr int64_t kMaxRaysPerEmitter = 1ll << 46;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct PinBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMallocHost(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+}  // namespace
+
+struct rf_ctx {
+    rf_config cfg{};
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+
+    // scene
+    int32_t n = 0, nbv = 0;
+    std::vector<rf_primitive> prims;
+    DevBuf d_tab, d_emit, d_bvtab, d_bvinfo;
+
+    // trace state
+    DevBuf d_hits, d_seg, d_rays, d_F, d_rec, d_err, d_misc;
+    PinBuf h_seg, h_rays, h_misc;
+    std::vector<int64_t> last_rays;
+    bool have_results = false;
+    int last_launches = 0;
+    bool timed = false;
+
+    // launch choices (0 = default); set by rf_config or rf_autotune
+    int block = 0, gpt = 0, hist = -1;
+};
+
+namespace {
+
+rf_status fail(rf_ctx *c, rf_status s, const char *fmt, ...)
+{
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return s;
+}
+
+rf_status cuda_fail(rf_ctx *c, cudaError_t e, const char *what)
+{
+    if (e == cudaErrorMemoryAllocation)
+        return fail(c, RF_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return fail(c, RF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define RF_CUDA(ctx, call)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+bool finite_all(const float *v, int k)
+{
+    for (int i = 0; i < k; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+bool uses_util1(int t) { return t == RF_FRUSTUM || t == RF_ANNULUS; }
+bool uses_util2(int t) { return t != RF_DISC && t != RF_RECTANGLE; }
+
+HitRec make_hitrec(const float *invm, int type, float util1, float util2)
+{
+    HitRec h;
+    h.r0 = make_float4(invm[0], invm[1], invm[2], invm[3]);
+    h.r1 = make_float4(invm[4], invm[5], invm[6], invm[7]);
+    h.r2 = make_float4(invm[8], invm[9], invm[10], invm[11]);
+    float t;
+    int32_t ti = type;
+    std::memcpy(&t, &ti, 4);
+    h.aux = make_float4(t, uses_util1(type) ? util1 : 0.f, uses_util2(type) ? util2 : 0.f, 0.f);
+    return h;
+}
+
+int arith_of(const rf_ctx *c)
+{
+    return (int)c->cfg.precision;
+}
+
+// Occupancy of the kernel that will run; 0 when the query fails.
+int blocks_per_sm(int arith, const LaunchCfg &lc)
+{
+    switch (arith) {
+    case RF_PREC_EXACT: return trace_blocks_per_sm<MExact>(lc);
+    case RF_PREC_FAST: return trace_blocks_per_sm<MFast>(lc);
+    case RF_PREC_FP64: return trace_blocks_per_sm<MF64>(lc);
+    default: return trace_blocks_per_sm<MFast>(lc);
+    }
+}
+
+cudaError_t launch_arith(int arith, const LaunchCfg &lc, const TraceParams &p, cudaStream_t st)
+{
+    switch (arith) {
+    case RF_PREC_EXACT: return launch_trace<MExact>(lc, p, st);
+    case RF_PREC_FAST: return launch_trace<MFast>(lc, p, st);
+    case RF_PREC_FP64: return launch_trace<MF64>(lc, p, st);
+    default: return launch_trace<MFast>(lc, p, st);
+    }
+}
+
+rf_status check_budgets(rf_ctx *c, const int64_t *rays, int n)
+{
+    for (int e = 0; e < n; ++e) {
+        if (rays[e] < 0) return fail(c, RF_ERR_INVALID_ARG, "rays_per_emitter[%d] = %lld < 0", e, (long long)rays[e]);
+        if (rays[e] > kMaxRaysPerEmitter)
+            return fail(c, RF_ERR_OVERFLOW, "rays_per_emitter[%d] = %lld exceeds 2^46", e, (long long)rays[e]);
+        if ((c->cfg.compat & RF_COMPAT_STREAMS) && rays[e] > (4ll << 32))
+            return fail(c, RF_ERR_OVERFLOW,
+                        "emitter %d: %lld rays exceed the 2^32 draws of the reference stream key", e,
+                        (long long)rays[e]);
+    }
+    return RF_OK;
+}
+
+// Segments [first_ray, first_ray + count) per emitter, chunked by chunk_gids draws.
+int64_t plan_segments(std::vector<Segment> &seg, int emitter, int scene, int64_t first,
+                      int64_t count, int64_t chunk_gids, int64_t chunk0)
+{
+    if (count <= 0) return chunk0;
+    Segment s;
+    s.emitter = emitter;
+    s.scene = scene;
+    s.ray_begin = first;
+    s.ray_end = first + count;
+    s.chunk_begin = chunk0;
+    const int64_t g0 = first >> 2, g1 = (first + count + 3) >> 2;
+    const int64_t chunks = (g1 - g0 + chunk_gids - 1) / chunk_gids;
+    seg.push_back(s);
+    return chunk0 + chunks;
+}
+
+struct Plan {
+    LaunchCfg lc;
+    bool hist = false;
+};
+
+// Launch shape for the single-scene kernels.
+Plan make_plan(rf_ctx *c, bool bv, bool rec)
+{
+    Plan pl;
+    pl.lc.bv = bv;
+    pl.lc.rec = rec;
+    pl.lc.block = c->block > 0 ? c->block : (c->cfg.block_size > 0 ? c->cfg.block_size : kBlock);
+    pl.lc.block = std::max(32, std::min(kBlock, pl.lc.block / 32 * 32));
+    int gpt = c->gpt > 0 ? c->gpt : (c->cfg.rays_per_thread == 8 ? 2 : 1);
+    if (bv || rec || c->cfg.precision == RF_PREC_FP64) gpt = 1;
+    pl.lc.gpt = gpt;
+    pl.hist = !rec && (c->hist >= 0 ? c->hist == 1 : true) && c->n <= kHistMax;
+    const int tab = bv ? 0 : std::min(c->n, kTile);
+    pl.lc.smem = (size_t)tab * sizeof(HitRec) + (pl.hist ? (size_t)c->n * 4 : 0);
+    return pl;
+}
+
+rf_status run_trace(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_chunks, Plan &pl,
+                    int32_t *d_rec, int64_t rec_base, bool zero_hits)
+{
+    const int n = c->n;
+    if (zero_hits) RF_CUDA(c, cudaMemsetAsync(c->d_hits.p, 0, (size_t)n * n * 8, c->stream));
+    c->last_launches = 0;
+    c->timed = false;
+    if (seg.empty() || total_chunks == 0) return RF_OK;
+    RF_CUDA(c, c->h_seg.ensure(seg.size() * sizeof(Segment)));
+    RF_CUDA(c, c->d_seg.ensure(seg.size() * sizeof(Segment)));
+    // the pinned staging buffer may still feed an earlier copy
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::memcpy(c->h_seg.p, seg.data(), seg.size() * sizeof(Segment));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_seg.p, c->h_seg.p, seg.size() * sizeof(Segment),
+                               cudaMemcpyHostToDevice, c->stream));
+
+    TraceParams p{};
+    p.tab = c->d_tab.as<HitRec>();
+    p.emit = c->d_emit.as<rf_primitive>();
+    p.bvtab = c->d_bvtab.as<HitRec>();
+    p.bvinfo = c->d_bvinfo.as<int4>();
+    p.seg = c->d_seg.as<Segment>();
+    p.hits = c->d_hits.as<unsigned long long>();
+    p.rec = d_rec;
+    p.rec_base = rec_base;
+    p.err = c->d_err.as<int32_t>();
+    p.total_chunks = total_chunks;
+    p.nseg = (int32_t)seg.size();
+    p.n = n;
+    p.nbv = c->nbv;
+    p.compat = c->cfg.compat;
+    p.key1 = c->cfg.key1;
+    p.scene_id = c->cfg.scene_id;
+    p.eps = c->cfg.eps;
+    p.use_smem_hist = pl.hist ? 1 : 0;
+
+    const int arith = arith_of(c);
+    int bps = blocks_per_sm(arith, pl.lc);
+    if (bps <= 0) bps = 1;
+    const int64_t wave = (int64_t)c->sms * bps;
+    pl.lc.grid = (int)std::max<int64_t>(1, std::min<int64_t>(wave, total_chunks));
+    RF_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    RF_CUDA(c, launch_arith(arith, pl.lc, p, c->stream));
+    RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    c->last_launches = 1;
+    c->timed = true;
+    return RF_OK;
+}
+
+rf_status require_scene(rf_ctx *c)
+{
+    if (!c) return RF_ERR_INVALID_ARG;
+    if (c->n <= 0) return fail(c, RF_ERR_STATE, "no scene: call rf_set_scene first");
+    return RF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rf_config_default(rf_config *cfg)
+{
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof *cfg);
+    cfg->struct_size = sizeof(rf_config);
+    cfg->compat = 0;
+    cfg->precision = RF_PREC_EXACT;
+    cfg->key1 = 0xdecafbadu;  // RayFactorGPU.cl:486
+    cfg->eps = 1e-3f;         // RayFactorGPU.cl:7
+    cfg->device = 0;
+}
+
+int32_t rf_abi_version(void) { return RF_ABI_VERSION; }
+
+const char *rf_status_string(rf_status s)
+{
+    switch (s) {
+    case RF_OK: return "ok";
+    case RF_ERR_INVALID_ARG: return "invalid argument";
+    case RF_ERR_BAD_SCENE: return "bad scene";
+    case RF_ERR_OOM: return "out of memory";
+    case RF_ERR_CUDA: return "CUDA error";
+    case RF_ERR_TIMEOUT: return "device wait timed out";
+    case RF_ERR_OVERFLOW: return "size overflow";
+    case RF_ERR_NO_DEVICE: return "no CUDA device";
+    case RF_ERR_UNSUPPORTED: return "unsupported";
+    case RF_ERR_STATE: return "wrong call order";
+    }
+    return "unknown status";
+}
+
+rf_status rf_create(rf_ctx **out, const rf_config *cfg)
+{
+    if (!out) return RF_ERR_INVALID_ARG;
+    *out = nullptr;
+    rf_config c;
+    rf_config_default(&c);
+    if (cfg) {
+        if (cfg->struct_size != sizeof(rf_config)) return RF_ERR_INVALID_ARG;
+        c = *cfg;
+    }
+    if (c.precision > RF_PREC_FP64) return RF_ERR_INVALID_ARG;
+    if (!(c.eps >= 0.0f) || !std::isfinite(c.eps)) return RF_ERR_INVALID_ARG;
+    if (c.rays_per_thread != 0 && c.rays_per_thread != 4 && c.rays_per_thread != 8)
+        return RF_ERR_INVALID_ARG;
+    if (c.block_size < 0 || c.block_size > kBlock || (c.block_size % 32) != 0) return RF_ERR_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return RF_ERR_NO_DEVICE;
+    }
+    if (c.device < 0 || c.device >= ndev) return RF_ERR_NO_DEVICE;
+    rf_ctx *ctx = new (std::nothrow) rf_ctx;
+    if (!ctx) return RF_ERR_OOM;
+    ctx->cfg = c;
+    ctx->device = c.device;
+    if (cudaSetDevice(c.device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        ctx->d_err.ensure(64) != cudaSuccess ||
+        cudaMemset(ctx->d_err.p, 0, 64) != cudaSuccess) {
+        cudaGetLastError();
+        rf_destroy(ctx);
+        return RF_ERR_CUDA;
+    }
+    *out = ctx;
+    return RF_OK;
+}
+
+void rf_destroy(rf_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (DevBuf *b : {&c->d_tab, &c->d_emit, &c->d_bvtab, &c->d_bvinfo, &c->d_hits, &c->d_seg,
+                      &c->d_rays, &c->d_F, &c->d_rec, &c->d_err, &c->d_misc})
+        b->release();
+    c->h_seg.release();
+    c->h_rays.release();
+    c->h_misc.release();
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char *rf_last_error(const rf_ctx *c)
+{
+    if (!c) return "null context";
+    return c->err.c_str();
+}
+
+rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf_bounding_volume *bvs,
+                       int32_t nbv)
+{
+    if (!c) return RF_ERR_INVALID_ARG;
+    if (!prims || n <= 0) return fail(c, RF_ERR_INVALID_ARG, "empty scene (n_prims = %d)", n);
+    if (n > kMaxPrims) return fail(c, RF_ERR_OVERFLOW, "%d primitives exceed the limit %d", n, kMaxPrims);
+    if (nbv < 0 || (nbv > 0 && !bvs)) return fail(c, RF_ERR_INVALID_ARG, "bad bounding-volume arguments");
+    std::vector<HitRec> tab(n);
+    for (int i = 0; i < n; ++i) {
+        const rf_primitive &p = prims[i];
+        if (p.type < 0 || p.type > RF_DISC)
+            return fail(c, RF_ERR_BAD_SCENE, "primitive %d: type %d is not a surface", i, p.type);
+        if (!finite_all(p.m, 12) || !finite_all(p.invm, 12))
+            return fail(c, RF_ERR_BAD_SCENE, "primitive %d: non-finite transform", i);
+        if ((uses_util1(p.type) && !std::isfinite(p.util1)) || (uses_util2(p.type) && !std::isfinite(p.util2)))
+            return fail(c, RF_ERR_BAD_SCENE, "primitive %d: non-finite util1/util2", i);
+        tab[i] = make_hitrec(p.invm, p.type, p.util1, p.util2);
+    }
+    std::vector<HitRec> bvtab(std::max(nbv, 1));
+    std::vector<int4> bvinfo(std::max(nbv, 1));
+    for (int b = 0; b < nbv; ++b) {
+        const rf_bounding_volume &v = bvs[b];
+        if (v.type < 0 || v.type > RF_DISC)
+            return fail(c, RF_ERR_BAD_SCENE, "bounding volume %d: type %d is not a surface", b, v.type);
+        if (!finite_all(v.invm, 12))
+            return fail(c, RF_ERR_BAD_SCENE, "bounding volume %d: non-finite transform", b);
+        if ((uses_util1(v.type) && !std::isfinite(v.util1)))
+            return fail(c, RF_ERR_BAD_SCENE, "bounding volume %d: non-finite util1", b);
+        if (v.objStartIndex < 0 || v.objEndIndex < v.objStartIndex || v.objEndIndex > n)
+            return fail(c, RF_ERR_BAD_SCENE, "bounding volume %d: children [%d,%d) outside [0,%d)", b,
+                        v.objStartIndex, v.objEndIndex, n);
+        bvtab[b] = make_hitrec(v.invm, v.type, v.util1, v.util2);
+        bvinfo[b] = make_int4(v.settings, v.objStartIndex, v.objEndIndex, 0);
+    }
+    RF_CUDA(c, cudaSetDevice(c->device));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    RF_CUDA(c, c->d_tab.ensure(sizeof(HitRec) * n));
+    RF_CUDA(c, c->d_emit.ensure(sizeof(rf_primitive) * n));
+    RF_CUDA(c, c->d_bvtab.ensure(sizeof(HitRec) * bvtab.size()));
+    RF_CUDA(c, c->d_bvinfo.ensure(sizeof(int4) * bvinfo.size()));
+    RF_CUDA(c, c->d_hits.ensure((size_t)n * n * 8));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_tab.p, tab.data(), sizeof(HitRec) * n, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_emit.p, prims, sizeof(rf_primitive) * n, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_bvtab.p, bvtab.data(), sizeof(HitRec) * bvtab.size(),
+                               cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_bvinfo.p, bvinfo.data(), sizeof(int4) * bvinfo.size(),
+                               cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->prims.assign(prims, prims + n);
+    c->n = n;
+    c->nbv = nbv;
+    c->have_results = false;
+    return RF_OK;
+}
+
+rf_status rf_trace_async(rf_ctx *c, const int64_t *rays, int32_t use_bv)
+{
+    rf_status s = require_scene(c);
+    if (s != RF_OK) return s;
+    if (!rays) return fail(c, RF_ERR_INVALID_ARG, "rays_per_emitter is NULL");
+    if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
+    if ((s = check_budgets(c, rays, c->n)) != RF_OK) return s;
+    RF_CUDA(c, cudaSetDevice(c->device));
+    Plan pl = make_plan(c, use_bv != 0, false);
+    const int64_t chunk_gids = (int64_t)pl.lc.block * pl.lc.gpt;
+    std::vector<Segment> seg;
+    int64_t chunks = 0;
+    for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, 0, rays[e], chunk_gids, chunks);
+    c->last_rays.assign(rays, rays + c->n);
+    c->have_results = false;
+    if ((s = run_trace(c, seg, chunks, pl, nullptr, 0, true)) != RF_OK) return s;
+    c->have_results = true;
+    return RF_OK;
+}
+
+rf_status rf_read_results(rf_ctx *c, uint64_t *hits_out, double *F_out)
+{
+    rf_status s = require_scene(c);
+    if (s != RF_OK) return s;
+    if (!c->have_results) return fail(c, RF_ERR_STATE, "no trace to read");
+    RF_CUDA(c, cudaSetDevice(c->device));
+    const int n = c->n;
+    const size_t nn = (size_t)n * n;
+    if (F_out) {
+        RF_CUDA(c, c->d_rays.ensure(n * sizeof(int64_t)));
+        RF_CUDA(c, c->d_F.ensure(nn * sizeof(double)));
+        RF_CUDA(c, c->h_rays.ensure(n * sizeof(int64_t)));
+        RF_CUDA(c, cudaStreamSynchronize(c->stream));
+        std::memcpy(c->h_rays.p, c->last_rays.data(), n * sizeof(int64_t));
+        RF_CUDA(c, cudaMemcpyAsync(c->d_rays.p, c->h_rays.p, n * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                   c->stream));
+        RF_CUDA(c, launch_normalise_single(c->d_hits.as<unsigned long long>(), c->d_rays.as<int64_t>(), n,
+                                           c->d_F.as<double>(), c->stream));
+        RF_CUDA(c, cudaMemcpyAsync(F_out, c->d_F.p, nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (hits_out)
+        RF_CUDA(c, cudaMemcpyAsync(hits_out, c->d_hits.p, nn * 8, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    int32_t err = 0;
+    RF_CUDA(c, cudaMemcpy(&err, c->d_err.p, 4, cudaMemcpyDeviceToHost));
+    if (err) return fail(c, RF_ERR_TIMEOUT, "device reported error %d", err);
+    return RF_OK;
+}
+
+rf_status rf_trace(rf_ctx *c, const int64_t *rays, int32_t use_bv, uint64_t *hits_out, double *F_out)
+{
+    rf_status s = rf_trace_async(c, rays, use_bv);
+    if (s != RF_OK) return s;
+    return rf_read_results(c, hits_out, F_out);
+}
+
+void *rf_stream(rf_ctx *c) { return c ? static_cast<void *>(c->stream) : nullptr; }
+
+rf_status rf_last_trace_stats(rf_ctx *c, double *kernel_ms, int32_t *launches)
+{
+    if (!c) return RF_ERR_INVALID_ARG;
+    if (launches) *launches = c->last_launches;
+    if (kernel_ms) {
+        *kernel_ms = 0.0;
+        if (c->timed) {
+            RF_CUDA(c, cudaEventSynchronize(c->ev1));
+            float ms = 0.f;
+            RF_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            *kernel_ms = ms;
+        }
+    }
+    return RF_OK;
+}
+
+rf_status rf_trace_rays(rf_ctx *c, int32_t emitter, int64_t first_ray, int64_t n_rays, int32_t use_bv,
+                        int32_t *out)
+{
+    rf_status s = require_scene(c);
+    if (s != RF_OK) return s;
+    if (emitter < 0 || emitter >= c->n) return fail(c, RF_ERR_INVALID_ARG, "emitter %d out of range", emitter);
+    if (first_ray < 0 || n_rays < 0 || !out) return fail(c, RF_ERR_INVALID_ARG, "bad ray range");
+    if (n_rays > (1ll << 31)) return fail(c, RF_ERR_OVERFLOW, "at most 2^31 rays per call");
+    if (first_ray + n_rays > kMaxRaysPerEmitter) return fail(c, RF_ERR_OVERFLOW, "ray index beyond 2^46");
+    if ((c->cfg.compat & RF_COMPAT_STREAMS) && first_ray + n_rays > (4ll << 32))
+        return fail(c, RF_ERR_OVERFLOW, "ray index beyond the reference stream key");
+    if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
+    if (n_rays == 0) return RF_OK;
+    RF_CUDA(c, cudaSetDevice(c->device));
+    Plan pl = make_plan(c, use_bv != 0, true);
+    const int64_t chunk_gids = (int64_t)pl.lc.block * pl.lc.gpt;
+    std::vector<Segment> seg;
+    const int64_t chunks = plan_segments(seg, emitter, 0, first_ray, n_rays, chunk_gids, 0);
+    RF_CUDA(c, c->d_rec.ensure((size_t)n_rays * 4));
+    if ((s = run_trace(c, seg, chunks, pl, c->d_rec.as<int32_t>(), first_ray, false)) != RF_OK) return s;
+    RF_CUDA(c, cudaMemcpyAsync(out, c->d_rec.p, (size_t)n_rays * 4, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->have_results = false;  // the tallies were not produced by this call
+    return RF_OK;
+}
+
+rf_status rf_ray_budgets(const rf_primitive *prims, int32_t n, int32_t n_samples, uint32_t compat,
+                         int64_t *rays_out)
+{
+    if (!prims || n <= 0 || !rays_out || n_samples < 0) return RF_ERR_INVALID_ARG;
+    const int64_t wg = 128;  // WG_SIZE, RayFactorCL/util_opencl.h:52
+    for (int e = 0; e < n; ++e) {
+        // main.cpp:172 indexes the table with the device number (0 for one device)
+        const int64_t rd = (compat & RF_COMPAT_BUDGET) ? prims[0].rayDensity : prims[e].rayDensity;
+        const int64_t prod = rd * (int64_t)n_samples;
+        if (prod > INT32_MAX || prod < INT32_MIN) return RF_ERR_OVERFLOW;  // int overflow in the reference
+        const int64_t nt = (int64_t)((int32_t)prod / 4);
+        if (nt < 0) return RF_ERR_OVERFLOW;
+        const int64_t rem = nt % wg;
+        const int64_t nthreads = rem > wg / 2 ? nt + wg - rem : nt - rem;  // main.cpp:173
+        rays_out[e] = nthreads * 4;                                       // main.cpp:178
+    }
+    return RF_OK;
+}
+
+rf_status rf_run_gpurng(rf_ctx *c, int32_t n_samples, int32_t use_bv, int64_t *rays_out,
+                        uint64_t *hits_out, double *F_out)
+{
+    rf_status s = require_scene(c);
+    if (s != RF_OK) return s;
+    std::vector<int64_t> rays(c->n);
+    if ((s = rf_ray_budgets(c->prims.data(), c->n, n_samples, c->cfg.compat, rays.data())) != RF_OK)
+        return fail(c, s, "ray budget rayDensity*n_samples overflows int32 (main.cpp:172)");
+    if (rays_out) std::copy(rays.begin(), rays.end(), rays_out);
+    return rf_trace(c, rays.data(), use_bv, hits_out, F_out);
+}
+
+rf_status rf_write_output_txt(const char *path, const double *F, int32_t n)
+{
+    if (!path || !F || n <= 0) return RF_ERR_INVALID_ARG;
+    FILE *f = std::fopen(path, "w");
+    if (!f) return RF_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+            // the reference stores F as float and prints with precision 8 (main.cpp:216, 238-246)
+            std::fprintf(f, "%.8g,", (double)(float)F[(size_t)i * n + j]);
+        }
+        std::fputc('\n', f);
+    }
+    return std::fclose(f) == 0 ? RF_OK : RF_ERR_INVALID_ARG;
+}
+
+rf_status rf_check_F(rf_ctx *c, const double *F, const double *areas, int32_t n, double *max_sum_err,
+                     double *max_recip_err)
+{
+    if (!c || !F || n <= 0) return RF_ERR_INVALID_ARG;
+    RF_CUDA(c, cudaSetDevice(c->device));
+    const size_t nn = (size_t)n * n;
+    RF_CUDA(c, c->d_F.ensure(nn * sizeof(double)));
+    RF_CUDA(c, c->d_misc.ensure(n * sizeof(double) + 64));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_F.p, F, nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    double *d_areas = nullptr;
+    if (areas) {
+        d_areas = reinterpret_cast<double *>(static_cast<char *>(c->d_misc.p) + 64);
+        RF_CUDA(c, cudaMemcpyAsync(d_areas, areas, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
+    double *out2 = c->d_misc.as<double>();
+    RF_CUDA(c, launch_check_F(c->d_F.as<double>(), d_areas, n, out2, c->stream));
+    double h[2] = {0, 0};
+    RF_CUDA(c, cudaMemcpyAsync(h, out2, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (max_sum_err) *max_sum_err = h[0];
+    if (max_recip_err) *max_recip_err = h[1];
+    return RF_OK;
+}
+
+rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s)
+{
+    if (!fma_per_s) return RF_ERR_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return RF_ERR_NO_DEVICE;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return RF_ERR_CUDA;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int block = 256, grid = sms * 8, iters = 4096;
+    float *out = nullptr;
+    cudaEvent_t a, b;
+    if (cudaMalloc(&out, (size_t)grid * block * 4) != cudaSuccess) return RF_ERR_OOM;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    double best = 0.0;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(a);
+        launch_fp32_probe(out, iters, grid, block, 0);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        const double fmas = (double)grid * block * iters * 16.0 * 8.0;
+        if (rep > 0 && ms > 0) best = std::max(best, fmas / (ms * 1e-3));
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    if (e != cudaSuccess) return RF_ERR_CUDA;
+    *fma_per_s = best;
+    return RF_OK;
+}
+
+rf_status rf_trace_batch(rf_ctx *c, const rf_scene_desc *, int32_t, uint64_t *, double *)
+{
+    return fail(c, RF_ERR_UNSUPPORTED, "batched tracing not built in this library");
+}
+
+rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *, int32_t, double, int64_t, int32_t,
+                            uint64_t *, double *, int64_t *, int32_t *)
+{
+    return fail(c, RF_ERR_UNSUPPORTED, "batched tracing not built in this library");
+}
+
+rf_status rf_autotune(rf_ctx *c, int32_t, const char *)
+{
+    return fail(c, RF_ERR_UNSUPPORTED, "autotuner not built in this library");
+}
+
+rf_status rf_last_refine_count(rf_ctx *c, uint64_t *refined)
+{
+    if (!c || !refined) return RF_ERR_INVALID_ARG;
+    *refined = 0;
+    return RF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,99 @@
+// rf_internal.h -- structures shared by the host C ABI and the kernel
+// translation units.  Not part of the public interface.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rayfactor_gb300.h"
+
+namespace rf {
+
+// Hit-test record of one surface, 64 bytes, 16-byte aligned so that a block
+// stages the table into shared memory and reads it back as four 128-bit
+// broadcast loads: the three rows of invm (world->object) and
+// (type as int bits, util1, util2, 0).
+struct __align__(16) HitRec {
+    float4 r0, r1, r2, aux;
+};
+static_assert(sizeof(HitRec) == 64, "HitRec layout");
+
+// One contiguous ray range of one emitter.  Chunks of kChunkGids Philox
+// draws are numbered across segments; chunk_begin is their prefix sum.
+struct Segment {
+    int32_t emitter;     // primitive index within its scene
+    int32_t scene;       // scene index (0 for single-scene traces)
+    int64_t ray_begin;   // first ray (ray r uses draw r/4, rotation r%4)
+    int64_t ray_end;     // one past the last ray
+    int64_t chunk_begin; // first global chunk index of this segment
+};
+
+// Per-scene offsets for the batched kernel.
+struct SceneInfo {
+    int32_t n;           // primitives
+    int32_t prim_off;    // first record in the concatenated tables
+    int64_t hits_off;    // first tally of its n x n matrix
+};
+
+struct TraceParams {
+    const HitRec *tab;              // surface hit records, n (concatenated over scenes)
+    const rf_primitive *emit;       // reference-layout records (emission)
+    const HitRec *bvtab;            // bounding-surface hit records, nbv
+    const int4 *bvinfo;             // bounding surfaces: (settings, start, end, 0)
+    const Segment *seg;             // segments
+    const SceneInfo *scenes;        // batched kernel only
+    unsigned long long *hits;       // n x n tallies (or all scenes' matrices)
+    int32_t *rec;                   // per-ray hit index (record mode) or null
+    int64_t rec_base;               // ray index written to rec[0]
+    unsigned long long *refined;    // counter of FP64 re-evaluations (mixed)
+    unsigned long long *queue;      // work-queue head (batched kernel)
+    int32_t *err;                   // device error flag
+    int64_t total_chunks;
+    int32_t nseg;
+    int32_t n;                      // primitives (single-scene kernels)
+    int32_t nbv;
+    uint32_t compat;
+    uint32_t key1;
+    uint32_t scene_id;
+    float eps;
+    int32_t use_smem_hist;          // 1: shared-memory row histogram, 0: global atomics
+};
+
+constexpr int kBlock = 256;    // maximum threads per block of the single-scene kernels
+constexpr int kTile = 256;     // surface records per shared-memory tile (16 KB)
+constexpr int kHistMax = 8192; // largest row kept as a shared-memory histogram
+
+struct MExact;
+struct MFast;
+struct MF64;
+
+struct LaunchCfg {
+    int grid = 0;
+    int block = kBlock;
+    int gpt = 1;        // Philox draws per thread per chunk (4 rays each)
+    size_t smem = 0;
+    bool bv = false;    // runBVGPU semantics
+    bool rec = false;   // write per-ray hit indices instead of tallying
+};
+
+// Implemented once per arithmetic policy (rf_kern_exact.cu, rf_kern_fast.cu).
+template <class M> cudaError_t launch_trace(const LaunchCfg &cfg, const TraceParams &p, cudaStream_t st);
+template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
+
+// Batched mixed-precision persistent kernel (rf_kern_fast.cu).
+cudaError_t launch_batched(const TraceParams &p, int n_max, int grid, int block, size_t smem,
+                           cudaStream_t st);
+int batched_blocks_per_sm(int block, size_t smem);
+
+// FP64 post-processing and probes (rf_kern_post.cu).
+cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,
+                                    double *F, cudaStream_t st);
+cudaError_t launch_converge_step(const unsigned long long *hits, int64_t *rays,
+                                 const int64_t *row_off, const int32_t *row_n, int64_t nrows,
+                                 double *F, double tol, int64_t *next_rays, int64_t round_rays,
+                                 int32_t *not_converged, cudaStream_t st);
+cudaError_t launch_check_F(const double *F, const double *areas, int n, double *out2,
+                           cudaStream_t st);
+cudaError_t launch_fp32_probe(float *out, int iters, int grid, int block, cudaStream_t st);
+
+}  // namespace rf

@@ -1,0 +1,150 @@
+// rf_kern_post.cu -- FP64 post-processing of tallies on the device and the
+// FP32 issue-rate probe.
+//
+// The reference divides the summed int tallies by the rays shot on the host in
+// single precision (RayFactorCL/main.cpp:216-249).  Here the 64-bit tallies are
+// normalised in FP64 on the GPU, and the same pass computes each row's largest
+// binomial standard error sqrt(F(1-F)/rays) for the convergence loop.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rf_internal.h"
+
+namespace rf {
+
+// F[i] = hits[i] / rays[row(i)]; NaN for rows without rays (0/0 in main.cpp:245).
+__global__ void normalise_single_kernel(const unsigned long long *hits, const int64_t *rays, int n,
+                                        double *F)
+{
+    const int64_t total = (int64_t)n * n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = rays[i / n];
+        F[i] = (double)hits[i] / (double)r;
+    }
+}
+
+cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,
+                                    double *F, cudaStream_t st)
+{
+    const int64_t total = (int64_t)n * n;
+    int grid = (int)((total + 255) / 256);
+    if (grid > 4096) grid = 4096;
+    if (grid < 1) grid = 1;
+    normalise_single_kernel<<<grid, 256, 0, st>>>(hits, rays, n, F);
+    return cudaGetLastError();
+}
+
+// One warp per row of the batched tally: F, row standard error and the next
+// round's budget.  A row converges when max_j sqrt(F(1-F)/rays) <= tol.
+__global__ void converge_step_kernel(const unsigned long long *hits, int64_t *rays,
+                                     const int64_t *row_off, const int32_t *row_n, int64_t nrows,
+                                     double *F, double tol, int64_t *next_rays, int64_t round_rays,
+                                     int32_t *not_converged)
+{
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nrows) return;
+    const int64_t off = row_off[warp];
+    const int len = row_n[warp];
+    const int64_t r = rays[warp];
+    double worst = 0.0;
+    for (int j = lane; j < len; j += 32) {
+        const double f = r > 0 ? (double)hits[off + j] / (double)r : 0.0;
+        if (F) F[off + j] = r > 0 ? f : __longlong_as_double(0x7ff8000000000000ll);
+        const double var = r > 0 ? f * (1.0 - f) / (double)r : 1.0;
+        worst = fmax(worst, var);
+    }
+    for (int o = 16; o; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+    if (lane == 0) {
+        const bool more = sqrt(worst) > tol;
+        next_rays[warp] = more ? round_rays : 0;
+        if (more) atomicAdd(not_converged, 1);
+    }
+}
+
+cudaError_t launch_converge_step(const unsigned long long *hits, int64_t *rays,
+                                 const int64_t *row_off, const int32_t *row_n, int64_t nrows,
+                                 double *F, double tol, int64_t *next_rays, int64_t round_rays,
+                                 int32_t *not_converged, cudaStream_t st)
+{
+    const int64_t threads = nrows * 32;
+    int grid = (int)((threads + 255) / 256);
+    if (grid < 1) grid = 1;
+    converge_step_kernel<<<grid, 256, 0, st>>>(hits, rays, row_off, row_n, nrows, F, tol, next_rays,
+                                               round_rays, not_converged);
+    return cudaGetLastError();
+}
+
+__device__ __forceinline__ void atomic_max_double(double *a, double v)
+{
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long *>(a), (unsigned long long)__double_as_longlong(v));
+}
+
+// out2[0] = max_i |sum_j F_ij - 1|; out2[1] = max over pairs with both entries
+// non-zero of |A_i F_ij - A_j F_ji| / max(A_i F_ij, A_j F_ji).
+__global__ void check_F_kernel(const double *F, const double *areas, int n, double *out2)
+{
+    const int i = blockIdx.x;
+    double s = 0.0, worst = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double fij = F[(int64_t)i * n + j];
+        s += fij;
+        if (areas) {
+            const double fji = F[(int64_t)j * n + i];
+            const double a = areas[i] * fij, b = areas[j] * fji;
+            if (fij > 0.0 && fji > 0.0) worst = fmax(worst, fabs(a - b) / fmax(a, b));
+        }
+    }
+    __shared__ double ss[256], sw[256];
+    ss[threadIdx.x] = s;
+    sw[threadIdx.x] = worst;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o; o >>= 1) {
+        if (threadIdx.x < o) {
+            ss[threadIdx.x] += ss[threadIdx.x + o];
+            sw[threadIdx.x] = fmax(sw[threadIdx.x], sw[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomic_max_double(&out2[0], fabs(ss[0] - 1.0));
+        atomic_max_double(&out2[1], sw[0]);
+    }
+}
+
+cudaError_t launch_check_F(const double *F, const double *areas, int n, double *out2, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    check_F_kernel<<<n, 256, 0, st>>>(F, areas, n, out2);
+    return cudaGetLastError();
+}
+
+// Eight independent FMA chains per thread: the FP32 issue roofline.
+__global__ void fp32_probe_kernel(float *out, int iters)
+{
+    float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+    float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+    const float m = 0.999999f, c = 1e-7f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            a0 = __fmaf_rn(a0, m, c); a1 = __fmaf_rn(a1, m, c);
+            a2 = __fmaf_rn(a2, m, c); a3 = __fmaf_rn(a3, m, c);
+            a4 = __fmaf_rn(a4, m, c); a5 = __fmaf_rn(a5, m, c);
+            a6 = __fmaf_rn(a6, m, c); a7 = __fmaf_rn(a7, m, c);
+        }
+    }
+    const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 12345.678f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the chains live
+}
+
+cudaError_t launch_fp32_probe(float *out, int iters, int grid, int block, cudaStream_t st)
+{
+    fp32_probe_kernel<<<grid, block, 0, st>>>(out, iters);
+    return cudaGetLastError();
+}
+
+}  // namespace rf

@@ -1,0 +1,162 @@
+"""Host-side interface over the C ABI, mirroring the reference's host driver.
+
+:func:`run_cl_gpurng` has the signature and the behaviour of
+``runCL_GPURNG(int n_samples, Scene &scene)`` (RayFactorCL/main.cpp:54-272):
+it sizes each emitter's ray budget (main.cpp:172-173), chooses the
+bounding-surface kernel when the scene asks for it (main.cpp:68-75), traces,
+normalises the tallies by the rays shot (main.cpp:178, 241-249) and writes
+``output.txt`` (main.cpp:236-249).  :class:`Tracer` exposes the individual
+steps.  All work runs in the CUDA library; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import _lib
+from ._lib import (COMPAT_ALL, COMPAT_BUDGET, COMPAT_BV_STALE, COMPAT_SPHERE, COMPAT_STREAMS,  # noqa: F401
+                   PREC_EXACT, PREC_FAST, PREC_MIXED, PREC_FP64, RfError, check, ptr)
+from .scene import BV_DTYPE, PRIM_DTYPE, Scene
+
+REF_KEY1 = 0xDECAFBAD
+
+
+class Tracer:
+    """One CUDA context (stream, device buffers) holding one scene."""
+
+    def __init__(self, precision: int = PREC_EXACT, compat: int = 0, key1: int = REF_KEY1,
+                 eps: float = 1e-3, device: int = 0, block_size: int = 0, rays_per_thread: int = 0,
+                 scene_id: int = 0):
+        L = _lib.load()
+        cfg = _lib.RfConfig()
+        L.rf_config_default(ctypes.byref(cfg))
+        cfg.compat = compat
+        cfg.precision = precision
+        cfg.key1 = key1 & 0xFFFFFFFF
+        cfg.eps = eps
+        cfg.device = device
+        cfg.block_size = block_size
+        cfg.rays_per_thread = rays_per_thread
+        cfg.scene_id = scene_id & 0xFFFFFFFF
+        h = ctypes.c_void_p()
+        check(L.rf_create(ctypes.byref(h), ctypes.byref(cfg)))
+        self._h = h
+        self._L = L
+        self.cfg = cfg
+        self.n = 0
+        self.scene: Scene | None = None
+
+    # -- lifetime --------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.rf_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, status):
+        check(status, self._h)
+
+    # -- scene -----------------------------------------------------------
+    def set_scene(self, scene: Scene):
+        prims = np.ascontiguousarray(scene.primitives, PRIM_DTYPE)
+        bvs = np.ascontiguousarray(scene.bounding_volumes, BV_DTYPE)
+        self._check(self._L.rf_set_scene(self._h, ptr(prims), prims.shape[0],
+                                         ptr(bvs) if bvs.shape[0] else None, bvs.shape[0]))
+        self.n = prims.shape[0]
+        self.scene = scene
+
+    # -- tracing ---------------------------------------------------------
+    def _rays(self, rays) -> np.ndarray:
+        r = np.ascontiguousarray(np.broadcast_to(np.asarray(rays, np.int64), (self.n,)), np.int64)
+        return r
+
+    def trace(self, rays, use_bv: bool = False, want_F: bool = True):
+        """Tally matrix (int64 n x n) and F (float64 n x n, or None)."""
+        r = self._rays(rays)
+        hits = np.zeros((self.n, self.n), np.uint64)
+        F = np.zeros((self.n, self.n), np.float64) if want_F else None
+        self._check(self._L.rf_trace(self._h, ptr(r), 1 if use_bv else 0, ptr(hits), ptr(F)))
+        return hits.astype(np.int64), F
+
+    def trace_async(self, rays, use_bv: bool = False):
+        self._keep = self._rays(rays)
+        self._check(self._L.rf_trace_async(self._h, ptr(self._keep), 1 if use_bv else 0))
+
+    def read_results(self, hits: np.ndarray | None = None, F: np.ndarray | None = None):
+        self._check(self._L.rf_read_results(self._h, ptr(hits), ptr(F)))
+        return hits, F
+
+    @property
+    def stream_handle(self) -> int:
+        """The context's cudaStream_t as an integer."""
+        return int(self._L.rf_stream(self._h) or 0)
+
+    def last_stats(self):
+        ms = ctypes.c_double()
+        launches = ctypes.c_int32()
+        self._check(self._L.rf_last_trace_stats(self._h, ctypes.byref(ms), ctypes.byref(launches)))
+        return ms.value, launches.value
+
+    def trace_rays(self, emitter: int, first_ray: int, n_rays: int, use_bv: bool = False) -> np.ndarray:
+        out = np.empty(n_rays, np.int32)
+        self._check(self._L.rf_trace_rays(self._h, emitter, first_ray, n_rays, 1 if use_bv else 0,
+                                          ptr(out)))
+        return out
+
+    def run_gpurng(self, n_samples: int, use_bv: bool = False):
+        rays = np.zeros(self.n, np.int64)
+        hits = np.zeros((self.n, self.n), np.uint64)
+        F = np.zeros((self.n, self.n), np.float64)
+        self._check(self._L.rf_run_gpurng(self._h, int(n_samples), 1 if use_bv else 0, ptr(rays),
+                                          ptr(hits), ptr(F)))
+        return rays, hits.astype(np.int64), F
+
+    def check_F(self, F: np.ndarray, areas: np.ndarray | None = None):
+        F = np.ascontiguousarray(F, np.float64)
+        a = None if areas is None else np.ascontiguousarray(areas, np.float64)
+        s, r = ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.rf_check_F(self._h, ptr(F), ptr(a), F.shape[0], ctypes.byref(s),
+                                       ctypes.byref(r)))
+        return s.value, r.value
+
+
+def ray_budgets(scene: Scene, n_samples: int, compat: int = 0) -> np.ndarray:
+    """main.cpp:172-173 budgets (rays, int64) for every emitter; no GPU needed."""
+    L = _lib.load()
+    prims = np.ascontiguousarray(scene.primitives, PRIM_DTYPE)
+    out = np.zeros(prims.shape[0], np.int64)
+    check(L.rf_ray_budgets(ptr(prims), prims.shape[0], int(n_samples), compat, ptr(out)))
+    return out
+
+
+def write_output_txt(path: str | Path, F: np.ndarray):
+    """main.cpp:236-249 format: rows of '%.8g,' values."""
+    F = np.ascontiguousarray(F, np.float64)
+    check(_lib.load().rf_write_output_txt(str(path).encode(), ptr(F), F.shape[0]))
+
+
+def run_cl_gpurng(n_samples: int, scene: Scene, output: str | Path | None = "output.txt",
+                  **tracer_kw):
+    """runCL_GPURNG(n_samples, scene) (main.cpp:54-272) on the GPU.
+
+    Returns (rays per emitter, int64 tallies, F).  Writes ``output`` unless it is None.
+    """
+    with Tracer(**tracer_kw) as t:
+        t.set_scene(scene)
+        rays, hits, F = t.run_gpurng(n_samples, use_bv=bool(scene.use_bounding_volumes))
+    if output is not None:
+        write_output_txt(output, F)
+    return rays, hits, F
