@@ -117,11 +117,16 @@ def cpu_rate(w, seconds: float, threads: int = 0):
     """Oracle rays/s on host cores over a bounded, area-weighted sample."""
     from oracle import oracle as O
     p = O.params(compat=0, key1=w.key1)
-    probe = np.maximum((w.rays // 20000) // 4 * 4, 4)
-    t0 = time.perf_counter()
-    O.tally(w.scene, p, probe, threads=threads)
-    dt = time.perf_counter() - t0
-    scale = max(1.0, seconds / max(dt, 1e-3))
+    frac = 1e-4
+    while True:
+        probe = np.maximum((w.rays * frac).astype(np.int64) // 4 * 4, 4)
+        t0 = time.perf_counter()
+        O.tally(w.scene, p, probe, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt > 0.5 or frac >= 1.0:
+            break
+        frac *= 8
+    scale = seconds / max(dt, 1e-3)
     sample = np.maximum((probe * scale).astype(np.int64) // 4 * 4, 4)
     t0 = time.perf_counter()
     O.tally(w.scene, p, sample, threads=threads)
@@ -189,7 +194,7 @@ def run_ours(args):
             dist.barrier()
 
     # -- value: scene resident, per-step device time ----------------------
-    t = Tracer(precision=prec, key1=w.key1, device=local)
+    t = Tracer(precision=prec, key1=w.key1, device=local, rays_per_thread=args.rays_per_thread)
     t.set_scene(sc)
     stream = torch.cuda.ExternalStream(t.stream_handle, device=f"cuda:{local}")
     for _ in range(args.warmup):
@@ -290,6 +295,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="exact", choices=["exact", "fast"])
     ap.add_argument("--rays", type=int, default=100_000_000)
+    ap.add_argument("--rays-per-thread", type=int, default=0, choices=[0, 4, 8])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -80,8 +80,12 @@ class Tracer:
 
     # -- tracing ---------------------------------------------------------
     def _rays(self, rays) -> np.ndarray:
-        r = np.ascontiguousarray(np.broadcast_to(np.asarray(rays, np.int64), (self.n,)), np.int64)
-        return r
+        r = np.asarray(rays, np.int64)
+        if self.n and r.ndim == 0:
+            r = np.broadcast_to(r, (self.n,))
+        if self.n and r.shape != (self.n,):
+            raise ValueError(f"rays_per_emitter needs {self.n} entries, got {r.shape}")
+        return np.ascontiguousarray(r, np.int64)
 
     def trace(self, rays, use_bv: bool = False, want_F: bool = True):
         """Tally matrix (int64 n x n) and F (float64 n x n, or None)."""
