@@ -163,87 +163,137 @@ def run_reference(args):
     return 0
 
 
+def time_trace(t, rays, steps, warmup, l2_flush, stream):
+    """Per-step device time (CUDA events on the library's stream, L2 flushed
+    before each step) and the tracing kernel's own time."""
+    import torch
+    for _ in range(warmup):
+        t.trace_async(rays)
+        torch.cuda.synchronize()
+    step_ms, kern_ms = [], []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            l2_flush.zero_()  # inputs are smaller than L2: flush it between steps
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        t.trace_async(rays)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        kern_ms.append(t.last_stats()[0])
+    return float(np.mean(step_ms)), float(np.mean(kern_ms))
+
+
 def run_ours(args):
+    import ctypes
+
     import torch
 
     from rayfactorcl_gb300 import _lib
-    from rayfactorcl_gb300.tracer import PREC_EXACT, PREC_FAST, Tracer
+    from rayfactorcl_gb300.tracer import PREC_EXACT, PREC_FAST, PREC_FP64, PREC_MIXED, Tracer
 
     rank, world, local = dist_info()
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
     _lib.load()
     w = workload(args)
     sc = w.scene
     rays = w.rays
     total_rays = int(rays.sum())
-    ops = algorithmic_ops(sc, rays)
-    prec = {"exact": PREC_EXACT, "fast": PREC_FAST}[args.precision]
+    ref_ops = algorithmic_ops(sc, rays)
+    headline = {"mixed": PREC_MIXED, "exact": PREC_EXACT, "fast": PREC_FAST}[args.precision]
 
-    fma = __import__("ctypes").c_double()
+    fma = ctypes.c_double()
     _lib.check(_lib.load().rf_measure_fp32_peak(local, fma))
     peak_ops = fma.value
-
-    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    # -- value: scene resident, per-step device time ----------------------
-    t = Tracer(precision=prec, key1=w.key1, device=local, rays_per_thread=args.rays_per_thread)
-    t.set_scene(sc)
-    stream = torch.cuda.ExternalStream(t.stream_handle, device=f"cuda:{local}")
-    for _ in range(args.warmup):
-        t.trace_async(rays)
-        torch.cuda.synchronize()
-    step_ms, kern_ms = [], []
+    def tracer(prec):
+        t = Tracer(precision=prec, key1=w.key1, device=local, rays_per_thread=args.rays_per_thread)
+        t.set_scene(sc)
+        return t, torch.cuda.ExternalStream(t.stream_handle, device=dev)
+
+    # -- headline kernel: scene resident, per-step device time ------------
+    t, stream = tracer(headline)
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                l2_flush.zero_()  # inputs are smaller than L2: flush it between steps
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-            t.trace_async(rays)
-            with torch.cuda.stream(stream):
-                e1.record(stream)
-            e1.synchronize()
-            step_ms.append(e0.elapsed_time(e1))
-            kern_ms.append(t.last_stats()[0])
+        ms_step, kernel_ms = time_trace(t, rays, args.steps, args.warmup, l2_flush, stream)
         torch.cuda.synchronize()
     barrier()
     hits = np.zeros((sc.n, sc.n), np.uint64)
     t.read_results(hits, None)
     assert int(hits.sum()) <= total_rays
-    ms_step = float(np.mean(step_ms))
+    work = t.work_counts() if headline == PREC_MIXED else None
+    refined = t.refined_count() if headline == PREC_MIXED else 0
     if world > 1:
         import torch.distributed as dist
-        m = torch.tensor([ms_step], device=f"cuda:{local}")
+        m = torch.tensor([ms_step], device=dev)
         dist.all_reduce(m, op=dist.ReduceOp.MAX)
         ms_step = float(m.item())
     value = world * total_rays / (ms_step * 1e-3)
-    kernel_ms = float(np.mean(kern_ms))
-    achieved = ops / (kernel_ms * 1e-3)
 
-    # -- e2e: host buffers through the C ABI ----------------------------
-    F = np.zeros((sc.n, sc.n), np.float64)
+    # -- e2e: host buffers through the C ABI (scene upload, trace, FP64 F, read-back)
     e2e_ms = []
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         t.set_scene(sc)
-        h2, F2 = t.trace(rays)
+        t.trace(rays)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = e2e_ms[args.warmup:]
     h2d = sc.primitives.nbytes + sc.n * 64 + rays.nbytes + 32 * sc.n + 8 * sc.n
+    if headline == PREC_MIXED:
+        h2d += sc.n * (112 + 64 + 16)
     d2h = sc.n * sc.n * 16
     t.close()
+
+    # roofline of the headline kernel: FP32 work it performed / its time
+    if work is not None:
+        types = sc.primitives["type"].astype(int)
+        emit = float(sum(int(r) * EMIT_OPS[int(ty)] for r, ty in zip(rays, types)))
+        tests = float(sum(int(work[k]) * TEST_OPS[k] for k in range(6)))
+        cone = 20.0 * float(work[6])
+        done_ops = emit + tests + cone
+        all_pairs = float(total_rays) * sc.n
+        culled = 1.0 - float(sum(int(work[k]) for k in range(6))) / all_pairs
+    else:
+        done_ops, culled = ref_ops, 0.0
+    achieved = done_ops / (kernel_ms * 1e-3)
+
+    # -- the plain kernel (reference method, bit-exact) on the same rays -----
+    plain = None
+    if headline != PREC_EXACT and not args.no_plain:
+        tp, sp = tracer(PREC_EXACT)
+        p_step, p_kern = time_trace(tp, rays, args.steps, args.warmup, l2_flush, sp)
+        tp.close()
+        plain = {"value": world * total_rays / (p_step * 1e-3), "unit": "rays/s", "ms_per_step": p_step,
+                 "kernel_ms": p_kern, "roofline_frac": ref_ops / (p_kern * 1e-3) / peak_ops}
+
+    # -- F error at equal rays against the FP64 tracer (identical streams) ----
+    ferr = None
+    if not args.no_ferr:
+        sub = np.maximum((rays // args.ferr_div) // 4 * 4, 4)
+        Fs = {}
+        for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED), ("exact", PREC_EXACT)):
+            tt, _ = tracer(prec)
+            Fs[name] = tt.trace(sub)[1]
+            tt.close()
+        sig = np.sqrt(np.clip(Fs["fp64"] * (1 - Fs["fp64"]), 0, None) / sub[:, None])
+        ferr = {"rays": int(sub.sum()),
+                "max_abs_mixed_vs_fp64": float(np.max(np.abs(Fs["mixed"] - Fs["fp64"]))),
+                "max_abs_plain_vs_fp64": float(np.max(np.abs(Fs["exact"] - Fs["fp64"]))),
+                "max_binomial_sigma": float(sig.max())}
 
     # -- CPU baseline -----------------------------------------------------
     cpu = None
@@ -256,25 +306,33 @@ def run_ours(args):
     prof = ROOT / "profiles" / "traffic.json"
     if prof.exists():
         try:
-            traffic = json.loads(prof.read_text()).get(f"{args.precision}_plain_bytes_per_launch")
+            traffic = json.loads(prof.read_text()).get(f"{args.precision}_bytes_per_launch")
         except (ValueError, OSError):
             traffic = None
 
+    kname = {"mixed": "batched mixed-precision persistent kernel (rf::batched_kernel)",
+             "exact": "plain bit-exact kernel (rf::trace_kernel<MExact>)",
+             "fast": "plain FP32-approximation kernel (rf::trace_kernel<MFast>)"}[args.precision]
     line = {
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "mixed64 seed 2: 64 surfaces (16 cyl, 16 frustum, 12 disc, 10 annulus, "
                                "10 sphere), 1e8 rays/step spread by area",
-                   "kernel": f"plain ({args.precision})", "l2": "flushed between steps (256 MB write)",
+                   "kernel": kname, "l2": "flushed between steps (256 MB write)",
                    "rays_per_step": total_rays},
         "e2e": {"value": world * total_rays / (float(np.mean(e2e_ms)) * 1e-3), "unit": "rays/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "fp32-issue", "achieved": achieved / 1e12, "peak": peak_ops / 1e12,
-                     "unit": "Top/s (FP32, FMA = 1 op)", "frac": achieved / peak_ops,
+                     "unit": "Top/s (FP32 ops performed, FMA = 1 op)", "frac": achieved / peak_ops,
                      "traffic": traffic,
                      "peak_source": "measured in-run: dependent-FMA issue probe (rf_measure_fp32_peak)"},
         "kernel_ms": kernel_ms,
+        "plain_kernel": plain,
+        "speedup_vs_plain": (value / plain["value"]) if plain else None,
+        "culled_test_fraction": culled,
+        "fp64_refined_tests": refined,
+        "f_error": ferr,
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
         "gpu_launches": args.steps,
@@ -293,7 +351,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="exact", choices=["exact", "fast"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "exact", "fast"])
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-ferr", action="store_true")
+    ap.add_argument("--ferr-div", type=int, default=10)
     ap.add_argument("--rays", type=int, default=100_000_000)
     ap.add_argument("--rays-per-thread", type=int, default=0, choices=[0, 4, 8])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

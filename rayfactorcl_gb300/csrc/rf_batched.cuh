@@ -1,0 +1,448 @@
+// rf_batched.cuh -- the batched mixed-precision persistent tracing kernel.
+//
+// One launch traces any number of independent scenes.  Work items are chunks
+// of kBatchDraws*kBatchThreads Philox draws (4 rays each) of one (scene,
+// emitter) segment; a persistent grid pulls them from a device queue (an
+// atomic counter), so scenes of 10 and of 400 surfaces load-balance.
+//
+// Per chunk a block
+//   1. emits its 2048 rays with FP32 hardware approximations into shared memory
+//      (same streams and emission formulas as the plain kernel,
+//      RayFactorGPU.cl:298-443),
+//   2. counting-sorts them by direction cell (octahedral map, 8x8 cells in
+//      Morton order), so that 32 consecutive rays point roughly the same way,
+//   3. lets every warp take packets of 32 sorted rays: the packet's origin
+//      ball and direction cone are reduced across the warp, and a surface is
+//      tested only if the cone can reach the surface's bounding sphere (one
+//      warp-uniform test per packet and surface instead of 32 ray tests),
+//   4. evaluates the surviving tests in FP32; a quadric whose discriminant
+//      B^2 - AC lost more than 12 bits to cancellation is re-evaluated in FP64
+//      (counted), and
+//   5. tallies first hits in a shared-memory row histogram flushed as 64-bit
+//      atomics whenever the (scene, emitter) row changes.
+// Skipping a surface whose bounding sphere no ray of the packet can reach does
+// not change any ray's nearest hit; only the arithmetic differs from the
+// exact kernel.
+#pragma once
+
+#include "rf_device.cuh"
+
+namespace rf {
+
+constexpr int kBatchThreads = 256;
+constexpr int kBatchDraws = 2;                                   // draws per thread per chunk
+constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 2048
+constexpr int kCells = 64;                                       // direction cells
+constexpr int kBatchTile = 256;                                  // surfaces per staged tile
+constexpr int kBatchHist = 2048;                                 // rows up to this stay in smem
+constexpr float kCondRel = 1.0f / 4096.0f;                       // 12 bits of cancellation
+
+struct BatchSmem {
+    float ray[6][kChunkRays];           // sx sy sz cx cy cz, by local ray index
+    float tb[kChunkRays];               // best t, by sorted position
+    int bi[kChunkRays];                 // best surface, by sorted position
+    uint16_t perm[kChunkRays];          // sorted position -> local ray index
+    uint8_t key[kChunkRays];            // direction cell, kCells = invalid ray
+    int cnt[kCells + 2];
+    HitRec tab[kBatchTile];
+    float4 bs[kBatchTile];
+    int hist[kBatchHist];
+    rf_primitive emit;
+    int64_t chunk;
+};
+
+// Octahedral cell of a direction, 8x8 cells in Morton order.
+__device__ __forceinline__ int direction_cell(float x, float y, float z)
+{
+    const float inv = 1.0f / (fabsf(x) + fabsf(y) + fabsf(z) + 1e-30f);
+    float u = x * inv, v = y * inv;
+    if (z < 0.0f) {
+        const float uu = (1.0f - fabsf(v)) * copysignf(1.0f, u);
+        const float vv = (1.0f - fabsf(u)) * copysignf(1.0f, v);
+        u = uu;
+        v = vv;
+    }
+    int i = min(7, max(0, (int)((u + 1.0f) * 4.0f)));
+    int j = min(7, max(0, (int)((v + 1.0f) * 4.0f)));
+    int m = 0;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) m |= (((i >> b) & 1) << (2 * b)) | (((j >> b) & 1) << (2 * b + 1));
+    return m;
+}
+
+// Bounds of a packet of rays (one per lane; invalid lanes excluded).
+struct Packet {
+    float ox, oy, oz, rho;  // origin ball
+    float ax, ay, az;       // cone axis (unit)
+    float cos_t, sin_t;     // cone half-angle
+    bool cull;              // false: the cone is too wide to cull with
+};
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_min(float v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ Packet packet_bounds(const Ray<float> &r, bool valid, int nvalid)
+{
+    Packet pk;
+    const float w = valid ? 1.0f : 0.0f;
+    const float inv_n = 1.0f / (float)nvalid;
+    pk.ox = warp_sum(w * r.sx) * inv_n;
+    pk.oy = warp_sum(w * r.sy) * inv_n;
+    pk.oz = warp_sum(w * r.sz) * inv_n;
+    const float dx = r.sx - pk.ox, dy = r.sy - pk.oy, dz = r.sz - pk.oz;
+    pk.rho = sqrtf(warp_max(valid ? dx * dx + dy * dy + dz * dz : 0.0f));
+    const float ilen = rsqrtf(r.cx * r.cx + r.cy * r.cy + r.cz * r.cz);
+    const float nx = r.cx * ilen, ny = r.cy * ilen, nz = r.cz * ilen;
+    float ax = warp_sum(w * nx), ay = warp_sum(w * ny), az = warp_sum(w * nz);
+    const float al = sqrtf(ax * ax + ay * ay + az * az);
+    pk.cull = al > 1e-3f * (float)nvalid;
+    const float ial = pk.cull ? 1.0f / al : 0.0f;
+    pk.ax = ax * ial;
+    pk.ay = ay * ial;
+    pk.az = az * ial;
+    // widen by 1e-4 for rounding in the normalisation and the dot products
+    const float c = warp_min(valid ? nx * pk.ax + ny * pk.ay + nz * pk.az : 1.0f) - 1e-4f;
+    pk.cull = pk.cull && c > 0.0f;  // cones of 90 degrees or wider are not culled
+    pk.cos_t = c;
+    pk.sin_t = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+    // the butterfly sums may differ in the last bit between lanes: use lane 0's
+    pk.ox = __shfl_sync(0xffffffffu, pk.ox, 0);
+    pk.oy = __shfl_sync(0xffffffffu, pk.oy, 0);
+    pk.oz = __shfl_sync(0xffffffffu, pk.oz, 0);
+    pk.rho = __shfl_sync(0xffffffffu, pk.rho, 0);
+    pk.ax = __shfl_sync(0xffffffffu, pk.ax, 0);
+    pk.ay = __shfl_sync(0xffffffffu, pk.ay, 0);
+    pk.az = __shfl_sync(0xffffffffu, pk.az, 0);
+    pk.cos_t = __shfl_sync(0xffffffffu, pk.cos_t, 0);
+    pk.sin_t = __shfl_sync(0xffffffffu, pk.sin_t, 0);
+    pk.cull = __shfl_sync(0xffffffffu, (int)pk.cull, 0) != 0;
+    return pk;
+}
+
+// Can a ray starting in the packet's origin ball with a direction in its cone
+// reach the sphere (c, r)?  Conservative (a margin of 1e-4 relative).
+__device__ __forceinline__ bool packet_may_hit(const Packet &pk, const float4 s)
+{
+    if (!pk.cull) return true;
+    const float vx = s.x - pk.ox, vy = s.y - pk.oy, vz = s.z - pk.oz;
+    const float L2 = vx * vx + vy * vy + vz * vz;
+    const float R = (s.w + pk.rho) * 1.0001f + 1e-6f + 1e-5f * sqrtf(L2);
+    if (L2 <= R * R) return true;
+    const float va = vx * pk.ax + vy * pk.ay + vz * pk.az;
+    // angle(v, axis) <= theta + beta, sin(beta) = R / |v|, in cosines times |v|
+    return va >= pk.cos_t * sqrtf(L2 - R * R) - pk.sin_t * R;
+}
+
+// Mixed-precision tests: FP32 with hardware approximations; quadrics whose
+// discriminant is ill-conditioned are recomputed in FP64.
+__device__ __forceinline__ Ray<double> to_f64(const Ray<float> &w)
+{
+    Ray<double> d;
+    d.sx = w.sx; d.sy = w.sy; d.sz = w.sz;
+    d.cx = w.cx; d.cy = w.cy; d.cz = w.cz;
+    return d;
+}
+
+__device__ __forceinline__ bool ill_conditioned(float A, float B, float C)
+{
+    const float d = B * B - A * C;
+    return fabsf(d) < kCondRel * (B * B + fabsf(A * C));
+}
+
+__device__ __noinline__ float cylinder_f64(const HitRec &h, const Ray<float> &w, float eps)
+{
+    return (float)cylinder_hit<MF64>(h, to_f64(w), (double)eps);
+}
+__device__ __noinline__ float frustum_f64(const HitRec &h, const Ray<float> &w, float eps)
+{
+    return (float)frustum_hit<MF64>(h, to_f64(w), (double)eps);
+}
+__device__ __noinline__ float sphere_f64(const HitRec &h, const Ray<float> &w, float eps, bool sc)
+{
+    return (float)sphere_hit<MF64>(h, to_f64(w), (double)eps, sc);
+}
+
+__device__ __forceinline__ float cylinder_mixed(const HitRec &h, const Ray<float> &w, float eps, int &nref)
+{
+    const Ray<float> o = xfrm_ray<MFast>(h, w);
+    const float A = fmaf(o.cx, o.cx, o.cy * o.cy);
+    const float B = -fmaf(o.sx, o.cx, o.sy * o.cy);
+    const float C = fmaf(o.sx, o.sx, fmaf(o.sy, o.sy, -1.f));
+    if (ill_conditioned(A, B, C)) {
+        ++nref;
+        return cylinder_f64(h, w, eps);
+    }
+    const float disc = MFast::sqrt(B * B - A * C);
+    const float ra = MFast::rcp(A);
+    return quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
+}
+
+__device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float> &w, float eps, int &nref)
+{
+    const Ray<float> o = xfrm_ray<MFast>(h, w);
+    const float top = h.aux.y;
+    const float fdir = (top - 1.f) * o.cz;
+    const float fstart = (top - 1.f) * o.sz + 1.f;
+    const float A = fmaf(o.cx, o.cx, fmaf(o.cy, o.cy, -fdir * fdir));
+    const float B = -fmaf(o.sx, o.cx, fmaf(o.sy, o.cy, -fstart * fdir));
+    const float C = fmaf(o.sx, o.sx, fmaf(o.sy, o.sy, -fstart * fstart));
+    if (ill_conditioned(A, B, C)) {
+        ++nref;
+        return frustum_f64(h, w, eps);
+    }
+    const float disc = MFast::sqrt(B * B - A * C);
+    const float ra = MFast::rcp(A);
+    return quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
+}
+
+__device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> &w, float eps, bool sc,
+                                              int &nref)
+{
+    if (sc) return sphere_hit<MFast>(h, w, eps, true);  // reference quirk: no root to refine
+    const Ray<float> o = xfrm_ray<MFast>(h, w);
+    const float A = o.cx * o.cx + o.cy * o.cy + o.cz * o.cz;
+    const float B = o.cx * o.sx + o.cy * o.sy + o.cz * o.sz;
+    const float C = o.sx * o.sx + o.sy * o.sy + o.sz * o.sz - 1.0f;
+    if (ill_conditioned(A, B, C)) {
+        ++nref;
+        return sphere_f64(h, w, eps, false);
+    }
+    const float d2 = B * B - A * C;
+    if (!(d2 >= 0.f)) return MFast::inf();
+    const float d = MFast::sqrt(d2);
+    const float ra = MFast::rcp(A);
+    const float t1 = (-B - d) * ra, t2 = (-B + d) * ra;
+    if (t1 > eps) return t1;
+    if (t2 > eps) return t2;
+    return MFast::inf();
+}
+
+__device__ __forceinline__ float hit_mixed(int type, const HitRec &h, const Ray<float> &w, float eps,
+                                           bool sc, int &nref)
+{
+    switch (type) {
+    case RF_RECTANGLE: return rectangle_hit<MFast>(h, w, eps);
+    case RF_DISC: return disc_hit<MFast>(h, w, eps);
+    case RF_ANNULUS: return annulus_hit<MFast>(h, w, eps);
+    case RF_CYLINDER: return cylinder_mixed(h, w, eps, nref);
+    case RF_FRUSTUM: return frustum_mixed(h, w, eps, nref);
+    case RF_SPHERE: return sphere_mixed(h, w, eps, sc, nref);
+    default: return MFast::inf();
+    }
+}
+
+template <bool REC>
+__global__ void __launch_bounds__(kBatchThreads) batched_kernel(const TraceParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    BatchSmem &S = *reinterpret_cast<BatchSmem *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool sc = (p.compat & RF_COMPAT_SPHERE) != 0;
+    const float eps = p.eps;
+    const int64_t total = p.d_total ? *p.d_total : p.total_chunks;
+    const int nseg = p.d_nseg ? *p.d_nseg : p.nseg;
+
+    int cur_scene = -1, cur_emitter = -1;
+    SceneInfo si{};
+    int nref = 0;
+    // work counters (warp-uniform, counted by lane 0)
+    unsigned long long w_tests[6] = {0, 0, 0, 0, 0, 0}, w_cone = 0, w_packets = 0;
+    bool hist_on = false;
+
+    auto flush = [&]() {
+        __syncthreads();
+        if (hist_on && cur_emitter >= 0) {
+            unsigned long long *row = p.hits + si.hits_off + (int64_t)cur_emitter * si.n;
+            for (int i = tid; i < si.n; i += blockDim.x) {
+                const int v = S.hist[i];
+                if (v) {
+                    atomicAdd(row + i, (unsigned long long)v);
+                    S.hist[i] = 0;
+                }
+            }
+        }
+        __syncthreads();
+    };
+
+    for (;;) {
+        if (tid == 0) S.chunk = (int64_t)atomicAdd(p.queue, 1ull);
+        __syncthreads();
+        const int64_t c = S.chunk;
+        if (c >= total) break;  // block-uniform
+        const int s = find_segment(p.seg, nseg, c);
+        const Segment sg = p.seg[s];
+
+        if (sg.scene != cur_scene || sg.emitter != cur_emitter) {
+            if (!REC) flush();
+            if (sg.scene != cur_scene) {
+                si = p.scenes[sg.scene];
+                hist_on = !REC && si.n <= kBatchHist;
+                if (hist_on)
+                    for (int i = tid; i < si.n; i += blockDim.x) S.hist[i] = 0;
+                if (si.n <= kBatchTile) {  // resident table
+                    const float4 *src = reinterpret_cast<const float4 *>(p.tab + si.prim_off);
+                    float4 *dst = reinterpret_cast<float4 *>(S.tab);
+                    for (int i = tid; i < 4 * si.n; i += blockDim.x) dst[i] = __ldg(src + i);
+                    for (int i = tid; i < si.n; i += blockDim.x) S.bs[i] = __ldg(p.bsph + si.prim_off + i);
+                }
+                cur_scene = sg.scene;
+            }
+            if (tid < (int)(sizeof(rf_primitive) / 4))
+                reinterpret_cast<float *>(&S.emit)[tid] =
+                    reinterpret_cast<const float *>(p.emit + si.prim_off + sg.emitter)[tid];
+            cur_emitter = sg.emitter;
+        }
+        if (tid <= kCells) S.cnt[tid] = 0;
+        __syncthreads();
+
+        // 1. emission (draw d = g*blockDim + tid, ray l = 4d + v)
+        const int64_t gid0 = (sg.ray_begin >> 2) + (c - sg.chunk_begin) * (int64_t)(kBatchThreads * kBatchDraws);
+        const uint32_t sid = (p.compat & RF_COMPAT_STREAMS) ? 0u : (p.scene_id + (uint32_t)sg.scene);
+#pragma unroll
+        for (int g = 0; g < kBatchDraws; ++g) {
+            const int d = g * kBatchThreads + tid;
+            const int64_t gid = gid0 + d;
+            const uint4 u = stream_bits(p.compat, p.key1, sid, sg.emitter, gid);
+            const float uf[4] = {u01(u.x), u01(u.y), u01(u.z), u01(u.w)};
+#pragma unroll 1
+            for (int v = 0; v < 4; ++v) {
+                float r[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int q = (i + v + 1) & 3;
+                    r[i] = q == 0 ? uf[0] : (q == 1 ? uf[1] : (q == 2 ? uf[2] : uf[3]));
+                }
+                const Ray<float> ray = emit_ray<MFast>(S.emit, r);
+                const int l = 4 * d + v;
+                const int64_t rid = gid * 4 + v;
+                const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
+                S.ray[0][l] = ray.sx; S.ray[1][l] = ray.sy; S.ray[2][l] = ray.sz;
+                S.ray[3][l] = ray.cx; S.ray[4][l] = ray.cy; S.ray[5][l] = ray.cz;
+                const int key = valid ? direction_cell(ray.cx, ray.cy, ray.cz) : kCells;
+                S.key[l] = (uint8_t)key;
+                S.bi[l] = atomicAdd(&S.cnt[key], 1);  // rank within the bucket
+            }
+        }
+        __syncthreads();
+        // 2. counting sort: exclusive scan of the kCells+1 bucket sizes (warp 0)
+        if (warp == 0) {
+            const int a = S.cnt[lane], b = S.cnt[32 + lane];
+            int ia = a, ib = b;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int ta = __shfl_up_sync(0xffffffffu, ia, o);
+                const int tb2 = __shfl_up_sync(0xffffffffu, ib, o);
+                if (lane >= o) { ia += ta; ib += tb2; }
+            }
+            const int T1 = __shfl_sync(0xffffffffu, ia, 31);
+            const int T2 = __shfl_sync(0xffffffffu, ib, 31);
+            __syncwarp();
+            S.cnt[lane] = ia - a;
+            S.cnt[32 + lane] = T1 + ib - b;
+            if (lane == 0) S.cnt[kCells] = T1 + T2;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int g = 0; g < kBatchDraws; ++g)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const int l = 4 * (g * kBatchThreads + tid) + v;
+                S.perm[S.cnt[S.key[l]] + S.bi[l]] = (uint16_t)l;
+            }
+        __syncthreads();
+        for (int i = tid; i < kChunkRays; i += blockDim.x) {
+            S.tb[i] = MFast::inf();
+            S.bi[i] = -1;
+        }
+        __syncthreads();
+
+        // 3-4. packets of 32 sorted rays per warp, surfaces tile by tile
+        constexpr int kPackets = kChunkRays / 32 / (kBatchThreads / 32);  // per warp
+        const int ntiles = (si.n + kBatchTile - 1) / kBatchTile;
+        for (int tile = 0; tile < ntiles; ++tile) {
+            const int t0 = tile * kBatchTile;
+            const int cnt = min(kBatchTile, si.n - t0);
+            if (si.n > kBatchTile) {
+                __syncthreads();
+                const float4 *src = reinterpret_cast<const float4 *>(p.tab + si.prim_off + t0);
+                float4 *dst = reinterpret_cast<float4 *>(S.tab);
+                for (int i = tid; i < 4 * cnt; i += blockDim.x) dst[i] = __ldg(src + i);
+                for (int i = tid; i < cnt; i += blockDim.x) S.bs[i] = __ldg(p.bsph + si.prim_off + t0 + i);
+                __syncthreads();
+            }
+#pragma unroll 1
+            for (int k = 0; k < kPackets; ++k) {
+                const int pos = (warp * kPackets + k) * 32 + lane;
+                const int l = S.perm[pos];
+                const bool valid = S.key[l] < kCells;
+                const int nvalid = __popc(__ballot_sync(0xffffffffu, valid));
+                if (nvalid == 0) continue;
+                Ray<float> ray;
+                ray.sx = S.ray[0][l]; ray.sy = S.ray[1][l]; ray.sz = S.ray[2][l];
+                ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
+                const Packet pk = packet_bounds(ray, valid, nvalid);
+                float tb = S.tb[pos];
+                int bi = S.bi[pos];
+                w_cone += cnt;
+                ++w_packets;
+#pragma unroll 1
+                for (int jj = 0; jj < cnt; ++jj) {
+                    if (!packet_may_hit(pk, S.bs[jj])) continue;  // warp-uniform
+                    const HitRec h = S.tab[jj];
+                    const int type = __float_as_int(h.aux.x);
+                    if ((unsigned)type < 6u) w_tests[type] += nvalid;
+                    const float t = hit_mixed(type, h, ray, eps, sc, nref);
+                    if (t < tb) { tb = t; bi = t0 + jj; }
+                }
+                S.tb[pos] = tb;
+                S.bi[pos] = bi;
+            }
+        }
+        __syncthreads();
+        // 5. tally (or record) by sorted position; all rays of the chunk share one row
+        for (int pos = tid; pos < kChunkRays; pos += blockDim.x) {
+            const int l = S.perm[pos];
+            const bool valid = S.key[l] < kCells;
+            const int h = valid ? S.bi[pos] : -1;
+            if (REC) {
+                if (valid) p.rec[gid0 * 4 + l - p.rec_base] = h;
+            } else if (hist_on) {
+                warp_tally(S.hist, h);
+            } else {
+                warp_tally_global(p.hits + si.hits_off + (int64_t)cur_emitter * si.n, h);
+            }
+        }
+        __syncthreads();
+    }
+    if (!REC) flush();
+    // FP64 re-evaluations of this thread
+    int tot = nref;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if (lane == 0 && tot && p.refined) atomicAdd(p.refined, (unsigned long long)tot);
+    if (lane == 0 && p.work) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            if (w_tests[i]) atomicAdd(p.work + i, w_tests[i]);
+        atomicAdd(p.work + 6, w_cone);
+        atomicAdd(p.work + 7, w_packets);
+    }
+}
+
+}  // namespace rf

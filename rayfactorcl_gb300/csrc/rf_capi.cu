@@ -95,6 +95,14 @@ struct rf_ctx {
 
     // launch choices (0 = default); set by rf_config or rf_autotune
     int block = 0, gpt = 0, hist = -1;
+
+    // batched mixed-precision path: scenes concatenated, re-centred in FP64
+    DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters;
+    std::vector<SceneInfo> b_info;
+    int64_t b_hits_total = 0;
+    bool b_single = false;      // b_* hold the scene of rf_set_scene
+    unsigned long long last_refined = 0;
+    unsigned long long last_work[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -276,6 +284,183 @@ rf_status run_trace(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_ch
     return RF_OK;
 }
 
+rf_status validate_prims(rf_ctx *c, const rf_primitive *prims, int32_t n, int scene)
+{
+    if (!prims || n <= 0) return fail(c, RF_ERR_INVALID_ARG, "scene %d: empty (n_prims = %d)", scene, n);
+    if (n > kMaxPrims) return fail(c, RF_ERR_OVERFLOW, "scene %d: %d primitives exceed %d", scene, n, kMaxPrims);
+    for (int i = 0; i < n; ++i) {
+        const rf_primitive &p = prims[i];
+        if (p.type < 0 || p.type > RF_DISC)
+            return fail(c, RF_ERR_BAD_SCENE, "scene %d primitive %d: type %d is not a surface", scene, i, p.type);
+        if (!finite_all(p.m, 12) || !finite_all(p.invm, 12))
+            return fail(c, RF_ERR_BAD_SCENE, "scene %d primitive %d: non-finite transform", scene, i);
+        if ((uses_util1(p.type) && !std::isfinite(p.util1)) || (uses_util2(p.type) && !std::isfinite(p.util2)))
+            return fail(c, RF_ERR_BAD_SCENE, "scene %d primitive %d: non-finite util1/util2", scene, i);
+    }
+    return RF_OK;
+}
+
+// Mixed-precision tables of one scene.  The world origin moves (in FP64) to the
+// mean of the surfaces' translations, so a scene placed far from the origin keeps
+// its FP32 resolution: m' = m - anchor, invm' = invm o (x + anchor).  Each surface
+// also gets a conservative world bounding sphere (its object-space box mapped by m').
+void prepare_mixed(const rf_primitive *prims, int n, rf_primitive *emit, HitRec *tab, float4 *bs)
+{
+    double a[3] = {0, 0, 0};
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) a[k] += prims[i].m[4 * k + 3];
+    for (int k = 0; k < 3; ++k) a[k] /= n;
+    for (int i = 0; i < n; ++i) {
+        rf_primitive e = prims[i];
+        for (int k = 0; k < 3; ++k) {
+            e.m[4 * k + 3] = (float)((double)prims[i].m[4 * k + 3] - a[k]);
+            const float *r = prims[i].invm + 4 * k;
+            e.invm[4 * k + 3] = (float)((double)r[3] + (double)r[0] * a[0] + (double)r[1] * a[1] + (double)r[2] * a[2]);
+        }
+        emit[i] = e;
+        tab[i] = make_hitrec(e.invm, e.type, e.util1, e.util2);
+        double ext = 1.0, z0 = 0.0, z1 = 0.0;  // object-space box [-ext,ext]^2 x [z0,z1]
+        switch (e.type) {
+        case RF_CYLINDER: z1 = 1.0; break;
+        case RF_FRUSTUM: ext = std::max(1.0, std::fabs((double)e.util1)); z1 = 1.0; break;
+        case RF_SPHERE: z0 = -1.0; z1 = 1.0; break;
+        case RF_ANNULUS: ext = std::sqrt(std::max(0.0, (double)e.util2)); break;
+        default: break;
+        }
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, pts[8][3];
+        for (int q = 0; q < 8; ++q) {
+            const double o[3] = {(q & 1) ? ext : -ext, (q & 2) ? ext : -ext, (q & 4) ? z1 : z0};
+            for (int k = 0; k < 3; ++k) {
+                const float *r = e.m + 4 * k;
+                pts[q][k] = r[0] * o[0] + r[1] * o[1] + r[2] * o[2] + r[3];
+                lo[k] = std::min(lo[k], pts[q][k]);
+                hi[k] = std::max(hi[k], pts[q][k]);
+            }
+        }
+        const double cx = 0.5 * (lo[0] + hi[0]), cy = 0.5 * (lo[1] + hi[1]), cz = 0.5 * (lo[2] + hi[2]);
+        double rad = 0.0;
+        for (int q = 0; q < 8; ++q) {
+            const double dx = pts[q][0] - cx, dy = pts[q][1] - cy, dz = pts[q][2] - cz;
+            rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
+        }
+        const double cn = std::sqrt(cx * cx + cy * cy + cz * cz);
+        bs[i] = make_float4((float)cx, (float)cy, (float)cz, (float)(rad * (1.0 + 1e-5) + 1e-6 * (cn + rad) + 1e-7));
+    }
+}
+
+// Upload the scenes of a batch (one scene for rf_set_scene in MIXED mode).
+rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with_budgets)
+{
+    if (ns <= 0 || !scenes) return fail(c, RF_ERR_INVALID_ARG, "no scenes");
+    int64_t nprim = 0, nhits = 0;
+    for (int s = 0; s < ns; ++s) {
+        rf_status st = validate_prims(c, scenes[s].prims, scenes[s].n_prims, s);
+        if (st != RF_OK) return st;
+        if (with_budgets && !scenes[s].rays_per_emitter)
+            return fail(c, RF_ERR_INVALID_ARG, "scene %d: rays_per_emitter is NULL", s);
+        nprim += scenes[s].n_prims;
+        nhits += (int64_t)scenes[s].n_prims * scenes[s].n_prims;
+    }
+    if (nprim > (1ll << 31) / 4) return fail(c, RF_ERR_OVERFLOW, "too many surfaces in the batch");
+    std::vector<rf_primitive> emit(nprim);
+    std::vector<HitRec> tab(nprim);
+    std::vector<float4> bs(nprim);
+    c->b_info.resize(ns);
+    int64_t off = 0, hoff = 0;
+    for (int s = 0; s < ns; ++s) {
+        const int n = scenes[s].n_prims;
+        prepare_mixed(scenes[s].prims, n, emit.data() + off, tab.data() + off, bs.data() + off);
+        c->b_info[s].n = n;
+        c->b_info[s].prim_off = (int32_t)off;
+        c->b_info[s].hits_off = hoff;
+        off += n;
+        hoff += (int64_t)n * n;
+    }
+    RF_CUDA(c, cudaSetDevice(c->device));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    RF_CUDA(c, c->b_tab.ensure(sizeof(HitRec) * nprim));
+    RF_CUDA(c, c->b_emit.ensure(sizeof(rf_primitive) * nprim));
+    RF_CUDA(c, c->b_bsph.ensure(sizeof(float4) * nprim));
+    RF_CUDA(c, c->b_scenes.ensure(sizeof(SceneInfo) * ns));
+    RF_CUDA(c, c->b_hits.ensure((size_t)nhits * 8));
+    RF_CUDA(c, c->b_counters.ensure(256));
+    RF_CUDA(c, cudaMemcpyAsync(c->b_tab.p, tab.data(), sizeof(HitRec) * nprim, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->b_emit.p, emit.data(), sizeof(rf_primitive) * nprim, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->b_bsph.p, bs.data(), sizeof(float4) * nprim, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->b_scenes.p, c->b_info.data(), sizeof(SceneInfo) * ns, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->b_hits_total = nhits;
+    return RF_OK;
+}
+
+// Counters of the batched kernel inside b_counters.
+struct BatchCounters {
+    unsigned long long queue;
+    unsigned long long refined;
+    int64_t total;
+    int32_t nseg;
+    int32_t flags[2];  // not-converged rows, rounds
+    int32_t pad;
+    unsigned long long work[8];
+};
+
+TraceParams batch_params(rf_ctx *c)
+{
+    TraceParams p{};
+    BatchCounters *bc = c->b_counters.as<BatchCounters>();
+    p.tab = c->b_tab.as<HitRec>();
+    p.emit = c->b_emit.as<rf_primitive>();
+    p.bsph = c->b_bsph.as<float4>();
+    p.scenes = c->b_scenes.as<SceneInfo>();
+    p.hits = c->b_hits.as<unsigned long long>();
+    p.queue = &bc->queue;
+    p.refined = &bc->refined;
+    p.work = bc->work;
+    p.err = c->d_err.as<int32_t>();
+    p.compat = c->cfg.compat;
+    p.key1 = c->cfg.key1;
+    p.scene_id = c->cfg.scene_id;
+    p.eps = c->cfg.eps;
+    return p;
+}
+
+int batched_grid(rf_ctx *c, bool rec)
+{
+    int bps = batched_blocks_per_sm(rec);
+    if (bps <= 0) bps = 1;
+    return c->sms * bps;
+}
+
+// One persistent launch over host-planned segments.
+rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_chunks, bool rec,
+                      int32_t *d_rec, int64_t rec_base, bool zero_hits)
+{
+    c->last_launches = 0;
+    c->timed = false;
+    if (zero_hits) RF_CUDA(c, cudaMemsetAsync(c->b_hits.p, 0, (size_t)c->b_hits_total * 8, c->stream));
+    RF_CUDA(c, cudaMemsetAsync(c->b_counters.p, 0, sizeof(BatchCounters), c->stream));
+    if (seg.empty() || total_chunks == 0) return RF_OK;
+    RF_CUDA(c, c->h_seg.ensure(seg.size() * sizeof(Segment)));
+    RF_CUDA(c, c->d_seg.ensure(seg.size() * sizeof(Segment)));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::memcpy(c->h_seg.p, seg.data(), seg.size() * sizeof(Segment));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_seg.p, c->h_seg.p, seg.size() * sizeof(Segment), cudaMemcpyHostToDevice,
+                               c->stream));
+    TraceParams p = batch_params(c);
+    p.seg = c->d_seg.as<Segment>();
+    p.nseg = (int32_t)seg.size();
+    p.total_chunks = total_chunks;
+    p.rec = d_rec;
+    p.rec_base = rec_base;
+    const int grid = (int)std::min<int64_t>(batched_grid(c, rec), total_chunks);
+    RF_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    RF_CUDA(c, launch_batched(p, rec, grid, c->stream));
+    RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    c->last_launches = 1;
+    c->timed = true;
+    return RF_OK;
+}
+
 rf_status require_scene(rf_ctx *c)
 {
     if (!c) return RF_ERR_INVALID_ARG;
@@ -363,7 +548,8 @@ void rf_destroy(rf_ctx *c)
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (DevBuf *b : {&c->d_tab, &c->d_emit, &c->d_bvtab, &c->d_bvinfo, &c->d_hits, &c->d_seg,
-                      &c->d_rays, &c->d_F, &c->d_rec, &c->d_err, &c->d_misc})
+                      &c->d_rays, &c->d_F, &c->d_rec, &c->d_err, &c->d_misc, &c->b_tab, &c->b_emit,
+                      &c->b_bsph, &c->b_scenes, &c->b_hits, &c->b_rows, &c->b_counters})
         b->release();
     c->h_seg.release();
     c->h_rays.release();
@@ -384,20 +570,11 @@ rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf
                        int32_t nbv)
 {
     if (!c) return RF_ERR_INVALID_ARG;
-    if (!prims || n <= 0) return fail(c, RF_ERR_INVALID_ARG, "empty scene (n_prims = %d)", n);
-    if (n > kMaxPrims) return fail(c, RF_ERR_OVERFLOW, "%d primitives exceed the limit %d", n, kMaxPrims);
+    rf_status st = validate_prims(c, prims, n, 0);
+    if (st != RF_OK) return st;
     if (nbv < 0 || (nbv > 0 && !bvs)) return fail(c, RF_ERR_INVALID_ARG, "bad bounding-volume arguments");
     std::vector<HitRec> tab(n);
-    for (int i = 0; i < n; ++i) {
-        const rf_primitive &p = prims[i];
-        if (p.type < 0 || p.type > RF_DISC)
-            return fail(c, RF_ERR_BAD_SCENE, "primitive %d: type %d is not a surface", i, p.type);
-        if (!finite_all(p.m, 12) || !finite_all(p.invm, 12))
-            return fail(c, RF_ERR_BAD_SCENE, "primitive %d: non-finite transform", i);
-        if ((uses_util1(p.type) && !std::isfinite(p.util1)) || (uses_util2(p.type) && !std::isfinite(p.util2)))
-            return fail(c, RF_ERR_BAD_SCENE, "primitive %d: non-finite util1/util2", i);
-        tab[i] = make_hitrec(p.invm, p.type, p.util1, p.util2);
-    }
+    for (int i = 0; i < n; ++i) tab[i] = make_hitrec(prims[i].invm, prims[i].type, prims[i].util1, prims[i].util2);
     std::vector<HitRec> bvtab(std::max(nbv, 1));
     std::vector<int4> bvinfo(std::max(nbv, 1));
     for (int b = 0; b < nbv; ++b) {
@@ -432,6 +609,12 @@ rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf
     c->n = n;
     c->nbv = nbv;
     c->have_results = false;
+    c->b_single = false;
+    if (c->cfg.precision == RF_PREC_MIXED) {
+        rf_scene_desc d{prims, n, 0, nullptr};
+        if ((st = upload_batch(c, &d, 1, false)) != RF_OK) return st;
+        c->b_single = true;
+    }
     return RF_OK;
 }
 
@@ -443,13 +626,24 @@ rf_status rf_trace_async(rf_ctx *c, const int64_t *rays, int32_t use_bv)
     if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
     if ((s = check_budgets(c, rays, c->n)) != RF_OK) return s;
     RF_CUDA(c, cudaSetDevice(c->device));
+    c->last_rays.assign(rays, rays + c->n);
+    c->have_results = false;
+    if (c->cfg.precision == RF_PREC_MIXED) {
+        if (use_bv) return fail(c, RF_ERR_UNSUPPORTED, "the mixed-precision kernel culls by bounding spheres; "
+                                                    "bounding-surface semantics need EXACT, FAST or FP64");
+        if (!c->b_single) return fail(c, RF_ERR_STATE, "scene not prepared for the mixed kernel");
+        std::vector<Segment> seg;
+        int64_t chunks = 0;
+        for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, 0, rays[e], kBatchChunkDraws, chunks);
+        if ((s = run_batched(c, seg, chunks, false, nullptr, 0, true)) != RF_OK) return s;
+        c->have_results = true;
+        return RF_OK;
+    }
     Plan pl = make_plan(c, use_bv != 0, false);
     const int64_t chunk_gids = (int64_t)pl.lc.block * pl.lc.gpt;
     std::vector<Segment> seg;
     int64_t chunks = 0;
     for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, 0, rays[e], chunk_gids, chunks);
-    c->last_rays.assign(rays, rays + c->n);
-    c->have_results = false;
     if ((s = run_trace(c, seg, chunks, pl, nullptr, 0, true)) != RF_OK) return s;
     c->have_results = true;
     return RF_OK;
@@ -463,6 +657,8 @@ rf_status rf_read_results(rf_ctx *c, uint64_t *hits_out, double *F_out)
     RF_CUDA(c, cudaSetDevice(c->device));
     const int n = c->n;
     const size_t nn = (size_t)n * n;
+    const unsigned long long *hits_dev = c->cfg.precision == RF_PREC_MIXED ? c->b_hits.as<unsigned long long>()
+                                                                           : c->d_hits.as<unsigned long long>();
     if (F_out) {
         RF_CUDA(c, c->d_rays.ensure(n * sizeof(int64_t)));
         RF_CUDA(c, c->d_F.ensure(nn * sizeof(double)));
@@ -471,12 +667,18 @@ rf_status rf_read_results(rf_ctx *c, uint64_t *hits_out, double *F_out)
         std::memcpy(c->h_rays.p, c->last_rays.data(), n * sizeof(int64_t));
         RF_CUDA(c, cudaMemcpyAsync(c->d_rays.p, c->h_rays.p, n * sizeof(int64_t), cudaMemcpyHostToDevice,
                                    c->stream));
-        RF_CUDA(c, launch_normalise_single(c->d_hits.as<unsigned long long>(), c->d_rays.as<int64_t>(), n,
-                                           c->d_F.as<double>(), c->stream));
+        RF_CUDA(c, launch_normalise_single(hits_dev, c->d_rays.as<int64_t>(), n, c->d_F.as<double>(),
+                                           c->stream));
         RF_CUDA(c, cudaMemcpyAsync(F_out, c->d_F.p, nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     }
-    if (hits_out)
-        RF_CUDA(c, cudaMemcpyAsync(hits_out, c->d_hits.p, nn * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (hits_out) RF_CUDA(c, cudaMemcpyAsync(hits_out, hits_dev, nn * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (c->cfg.precision == RF_PREC_MIXED)
+    {
+        RF_CUDA(c, cudaMemcpyAsync(&c->last_refined, &c->b_counters.as<BatchCounters>()->refined,
+                                   sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+        RF_CUDA(c, cudaMemcpyAsync(c->last_work, c->b_counters.as<BatchCounters>()->work,
+                                   sizeof c->last_work, cudaMemcpyDeviceToHost, c->stream));
+    }
     RF_CUDA(c, cudaStreamSynchronize(c->stream));
     int32_t err = 0;
     RF_CUDA(c, cudaMemcpy(&err, c->d_err.p, 4, cudaMemcpyDeviceToHost));
@@ -523,12 +725,19 @@ rf_status rf_trace_rays(rf_ctx *c, int32_t emitter, int64_t first_ray, int64_t n
     if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
     if (n_rays == 0) return RF_OK;
     RF_CUDA(c, cudaSetDevice(c->device));
-    Plan pl = make_plan(c, use_bv != 0, true);
-    const int64_t chunk_gids = (int64_t)pl.lc.block * pl.lc.gpt;
-    std::vector<Segment> seg;
-    const int64_t chunks = plan_segments(seg, emitter, 0, first_ray, n_rays, chunk_gids, 0);
     RF_CUDA(c, c->d_rec.ensure((size_t)n_rays * 4));
-    if ((s = run_trace(c, seg, chunks, pl, c->d_rec.as<int32_t>(), first_ray, false)) != RF_OK) return s;
+    if (c->cfg.precision == RF_PREC_MIXED) {
+        if (use_bv) return fail(c, RF_ERR_UNSUPPORTED, "bounding-surface semantics need EXACT, FAST or FP64");
+        std::vector<Segment> seg;
+        const int64_t chunks = plan_segments(seg, emitter, 0, first_ray, n_rays, kBatchChunkDraws, 0);
+        if ((s = run_batched(c, seg, chunks, true, c->d_rec.as<int32_t>(), first_ray, false)) != RF_OK) return s;
+    } else {
+        Plan pl = make_plan(c, use_bv != 0, true);
+        const int64_t chunk_gids = (int64_t)pl.lc.block * pl.lc.gpt;
+        std::vector<Segment> seg;
+        const int64_t chunks = plan_segments(seg, emitter, 0, first_ray, n_rays, chunk_gids, 0);
+        if ((s = run_trace(c, seg, chunks, pl, c->d_rec.as<int32_t>(), first_ray, false)) != RF_OK) return s;
+    }
     RF_CUDA(c, cudaMemcpyAsync(out, c->d_rec.p, (size_t)n_rays * 4, cudaMemcpyDeviceToHost, c->stream));
     RF_CUDA(c, cudaStreamSynchronize(c->stream));
     c->have_results = false;  // the tallies were not produced by this call
@@ -643,15 +852,163 @@ rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s)
     return RF_OK;
 }
 
-rf_status rf_trace_batch(rf_ctx *c, const rf_scene_desc *, int32_t, uint64_t *, double *)
+rf_status rf_trace_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_scenes, uint64_t *hits_out,
+                         double *F_out)
 {
-    return fail(c, RF_ERR_UNSUPPORTED, "batched tracing not built in this library");
+    if (!c) return RF_ERR_INVALID_ARG;
+    rf_status st = upload_batch(c, scenes, n_scenes, true);
+    if (st != RF_OK) return st;
+    c->b_single = false;
+    c->have_results = false;
+    std::vector<Segment> seg;
+    int64_t chunks = 0, nrows = 0;
+    for (int s = 0; s < n_scenes; ++s) {
+        if ((st = check_budgets(c, scenes[s].rays_per_emitter, scenes[s].n_prims)) != RF_OK) return st;
+        for (int e = 0; e < scenes[s].n_prims; ++e)
+            chunks = plan_segments(seg, e, s, 0, scenes[s].rays_per_emitter[e], kBatchChunkDraws, chunks);
+        nrows += scenes[s].n_prims;
+    }
+    if ((st = run_batched(c, seg, chunks, false, nullptr, 0, true)) != RF_OK) return st;
+    // FP64 normalisation of every row (one warp per row)
+    std::vector<int64_t> rows(3 * nrows);
+    int64_t r = 0;
+    for (int s = 0; s < n_scenes; ++s)
+        for (int e = 0; e < scenes[s].n_prims; ++e, ++r) {
+            rows[r] = c->b_info[s].hits_off + (int64_t)e * scenes[s].n_prims;     // row offset
+            rows[nrows + r] = scenes[s].rays_per_emitter[e];                      // rays
+            reinterpret_cast<int32_t *>(&rows[2 * nrows])[r] = scenes[s].n_prims;  // row length
+        }
+    RF_CUDA(c, c->b_rows.ensure(rows.size() * 8 + 8 * nrows));
+    RF_CUDA(c, c->d_F.ensure((size_t)c->b_hits_total * sizeof(double)));
+    int64_t *d_rows = c->b_rows.as<int64_t>();
+    RF_CUDA(c, cudaMemcpyAsync(d_rows, rows.data(), rows.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    BatchCounters *bc = c->b_counters.as<BatchCounters>();
+    RF_CUDA(c, launch_converge_step(c->b_hits.as<unsigned long long>(), d_rows + nrows, d_rows, 
+                                    reinterpret_cast<int32_t *>(d_rows + 2 * nrows), nrows,
+                                    c->d_F.as<double>(), 0.0, d_rows + 3 * nrows, 0, &bc->flags[0], c->stream));
+    if (hits_out)
+        RF_CUDA(c, cudaMemcpyAsync(hits_out, c->b_hits.p, (size_t)c->b_hits_total * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (F_out)
+        RF_CUDA(c, cudaMemcpyAsync(F_out, c->d_F.p, (size_t)c->b_hits_total * 8, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(&c->last_refined, &bc->refined, 8, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->last_work, bc->work, sizeof c->last_work, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return RF_OK;
 }
 
-rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *, int32_t, double, int64_t, int32_t,
-                            uint64_t *, double *, int64_t *, int32_t *)
+rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_scenes, double tol,
+                            int64_t round_rays, int32_t max_rounds, uint64_t *hits_out, double *F_out,
+                            int64_t *rays_out, int32_t *rounds_out)
 {
-    return fail(c, RF_ERR_UNSUPPORTED, "batched tracing not built in this library");
+    if (!c) return RF_ERR_INVALID_ARG;
+    if (!(tol > 0.0) || round_rays <= 0 || max_rounds <= 0)
+        return fail(c, RF_ERR_INVALID_ARG, "tol > 0, round_rays > 0 and max_rounds > 0 are required");
+    rf_status st = upload_batch(c, scenes, n_scenes, true);
+    if (st != RF_OK) return st;
+    c->b_single = false;
+    c->have_results = false;
+    int64_t nrows = 0;
+    for (int s = 0; s < n_scenes; ++s) {
+        if ((st = check_budgets(c, scenes[s].rays_per_emitter, scenes[s].n_prims)) != RF_OK) return st;
+        nrows += scenes[s].n_prims;
+    }
+    if ((int64_t)max_rounds * round_rays > kMaxRaysPerEmitter / 2)
+        return fail(c, RF_ERR_OVERFLOW, "max_rounds * round_rays is too large");
+    // row tables: off, rays_total, next, n | scene, emitter
+    std::vector<int64_t> off(nrows), next(nrows);
+    std::vector<int32_t> len(nrows), rsc(nrows), rem(nrows);
+    int64_t r = 0;
+    for (int s = 0; s < n_scenes; ++s)
+        for (int e = 0; e < scenes[s].n_prims; ++e, ++r) {
+            off[r] = c->b_info[s].hits_off + (int64_t)e * scenes[s].n_prims;
+            next[r] = scenes[s].rays_per_emitter[e];
+            len[r] = scenes[s].n_prims;
+            rsc[r] = s;
+            rem[r] = e;
+        }
+    RF_CUDA(c, c->b_rows.ensure((size_t)nrows * (8 * 3 + 4 * 3) + 64));
+    int64_t *d_off = c->b_rows.as<int64_t>(), *d_total = d_off + nrows, *d_next = d_total + nrows;
+    int32_t *d_len = reinterpret_cast<int32_t *>(d_next + nrows), *d_sc = d_len + nrows, *d_em = d_sc + nrows;
+    RF_CUDA(c, c->d_seg.ensure((size_t)nrows * sizeof(Segment)));
+    RF_CUDA(c, c->d_F.ensure((size_t)c->b_hits_total * sizeof(double)));
+    RF_CUDA(c, cudaMemcpyAsync(d_off, off.data(), nrows * 8, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemsetAsync(d_total, 0, nrows * 8, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(d_next, next.data(), nrows * 8, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(d_len, len.data(), nrows * 4, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(d_sc, rsc.data(), nrows * 4, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(d_em, rem.data(), nrows * 4, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemsetAsync(c->b_hits.p, 0, (size_t)c->b_hits_total * 8, c->stream));
+    RF_CUDA(c, cudaMemsetAsync(c->b_counters.p, 0, sizeof(BatchCounters), c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+
+    BatchCounters *bc = c->b_counters.as<BatchCounters>();
+    TraceParams p = batch_params(c);
+    p.seg = c->d_seg.as<Segment>();
+    p.d_total = &bc->total;
+    p.d_nseg = &bc->nseg;
+    const int grid = batched_grid(c, false);  // also sets the kernel's shared-memory attribute
+
+    // Graph: while (not converged && rounds < max) { plan; trace; converge; decide }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphConditionalHandle handle = 0;
+    auto body_ops = [&](unsigned long long h) -> cudaError_t {
+        cudaError_t e;
+        if ((e = launch_plan_round(nrows, d_sc, d_em, d_total, d_next, c->d_seg.as<Segment>(), &bc->nseg, &bc->total, &bc->queue,
+                                   kBatchChunkDraws, c->stream)) != cudaSuccess) return e;
+        if ((e = launch_batched(p, false, grid, c->stream)) != cudaSuccess) return e;
+        if ((e = launch_converge_step(c->b_hits.as<unsigned long long>(), d_total, d_off, d_len, nrows, nullptr,
+                                      tol, d_next, round_rays, &bc->flags[0], c->stream)) != cudaSuccess) return e;
+        return launch_decide_round(&bc->flags[0], max_rounds, h, c->stream);
+    };
+    cudaError_t e = cudaGraphCreate(&graph, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault);
+    cudaGraphNode_t node;
+    cudaGraphNodeParams np{};
+    if (e == cudaSuccess) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = handle;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+    }
+    if (e == cudaSuccess) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            cudaError_t e1 = body_ops((unsigned long long)handle);
+            cudaGraph_t captured = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(c->stream, &captured);
+            e = e1 != cudaSuccess ? e1 : e2;
+        }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e == cudaSuccess) {
+        RF_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+        e = cudaGraphLaunch(exec, c->stream);
+        RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "convergence graph");
+    c->timed = true;
+    c->last_launches = -1;  // rounds x 4 kernels, counted below
+    // final FP64 normalisation
+    RF_CUDA(c, launch_converge_step(c->b_hits.as<unsigned long long>(), d_total, d_off, d_len, nrows,
+                                    c->d_F.as<double>(), tol, d_next, 0, &bc->flags[0], c->stream));
+    int32_t flags[2] = {0, 0};
+    RF_CUDA(c, cudaMemcpyAsync(flags, &bc->flags[0], 8, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(&c->last_refined, &bc->refined, 8, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->last_work, bc->work, sizeof c->last_work, cudaMemcpyDeviceToHost, c->stream));
+    if (hits_out)
+        RF_CUDA(c, cudaMemcpyAsync(hits_out, c->b_hits.p, (size_t)c->b_hits_total * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (F_out)
+        RF_CUDA(c, cudaMemcpyAsync(F_out, c->d_F.p, (size_t)c->b_hits_total * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (rays_out) RF_CUDA(c, cudaMemcpyAsync(rays_out, d_total, nrows * 8, cudaMemcpyDeviceToHost, c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (rounds_out) *rounds_out = flags[1];
+    c->last_launches = 4 * flags[1];
+    return RF_OK;
 }
 
 rf_status rf_autotune(rf_ctx *c, int32_t, const char *)
@@ -659,10 +1016,17 @@ rf_status rf_autotune(rf_ctx *c, int32_t, const char *)
     return fail(c, RF_ERR_UNSUPPORTED, "autotuner not built in this library");
 }
 
+rf_status rf_last_work_counts(rf_ctx *c, uint64_t *counts)
+{
+    if (!c || !counts) return RF_ERR_INVALID_ARG;
+    for (int i = 0; i < 8; ++i) counts[i] = c->last_work[i];
+    return RF_OK;
+}
+
 rf_status rf_last_refine_count(rf_ctx *c, uint64_t *refined)
 {
     if (!c || !refined) return RF_ERR_INVALID_ARG;
-    *refined = 0;
+    *refined = c->last_refined;
     return RF_OK;
 }
 

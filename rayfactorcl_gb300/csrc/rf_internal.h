@@ -57,6 +57,11 @@ struct TraceParams {
     uint32_t scene_id;
     float eps;
     int32_t use_smem_hist;          // 1: shared-memory row histogram, 0: global atomics
+    const float4 *bsph;             // batched kernel: world bounding sphere per surface
+    const int64_t *d_total;         // batched kernel: device-resident chunk count (or null)
+    const int32_t *d_nseg;          // batched kernel: device-resident segment count (or null)
+    unsigned long long *work;       // batched kernel: [0..5] ray x surface tests by type,
+                                    // [6] packet x surface cone tests, [7] packets
 };
 
 constexpr int kBlock = 256;    // maximum threads per block of the single-scene kernels
@@ -81,9 +86,10 @@ template <class M> cudaError_t launch_trace(const LaunchCfg &cfg, const TracePar
 template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
 
 // Batched mixed-precision persistent kernel (rf_kern_fast.cu).
-cudaError_t launch_batched(const TraceParams &p, int n_max, int grid, int block, size_t smem,
-                           cudaStream_t st);
-int batched_blocks_per_sm(int block, size_t smem);
+cudaError_t launch_batched(const TraceParams &p, bool rec, int grid, cudaStream_t st);
+int batched_blocks_per_sm(bool rec);
+size_t batched_smem_bytes();
+constexpr int kBatchChunkDraws = 512;   // Philox draws per chunk of the batched kernel
 
 // FP64 post-processing and probes (rf_kern_post.cu).
 cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,
@@ -92,6 +98,11 @@ cudaError_t launch_converge_step(const unsigned long long *hits, int64_t *rays,
                                  const int64_t *row_off, const int32_t *row_n, int64_t nrows,
                                  double *F, double tol, int64_t *next_rays, int64_t round_rays,
                                  int32_t *not_converged, cudaStream_t st);
+cudaError_t launch_plan_round(int64_t nrows, const int32_t *row_scene, const int32_t *row_emitter,
+                              int64_t *rays_total, const int64_t *next, Segment *seg, int32_t *d_nseg,
+                              int64_t *d_total, unsigned long long *queue, int chunk_draws, cudaStream_t st);
+cudaError_t launch_decide_round(int32_t *flags, int32_t max_rounds, unsigned long long handle,
+                                cudaStream_t st);
 cudaError_t launch_check_F(const double *F, const double *areas, int n, double *out2,
                            cudaStream_t st);
 cudaError_t launch_fp32_probe(float *out, int iters, int grid, int block, cudaStream_t st);

@@ -76,6 +76,87 @@ cudaError_t launch_converge_step(const unsigned long long *hits, int64_t *rays,
     return cudaGetLastError();
 }
 
+// One round of the convergence loop, planned on the device: every row with
+// next[r] > 0 rays to add becomes a segment continuing its stream at
+// rays_total[r]; chunks are numbered across segments; the work queue is reset.
+__global__ void plan_round_kernel(int64_t nrows, const int32_t *row_scene, const int32_t *row_emitter,
+                                  int64_t *rays_total, const int64_t *next, Segment *seg, int32_t *d_nseg,
+                                  int64_t *d_total, unsigned long long *queue, int chunk_draws)
+{
+    __shared__ int64_t s_chunks[1024];
+    __shared__ int32_t s_nz[1024];
+    const int tid = threadIdx.x, T = blockDim.x;
+    const int64_t lo = nrows * tid / T, hi = nrows * (tid + 1) / T;
+    int64_t chunks = 0;
+    int32_t nz = 0;
+    for (int64_t r = lo; r < hi; ++r) {
+        const int64_t add = next[r];
+        if (add <= 0) continue;
+        const int64_t b = rays_total[r], g0 = b >> 2, g1 = (b + add + 3) >> 2;
+        chunks += (g1 - g0 + chunk_draws - 1) / chunk_draws;
+        ++nz;
+    }
+    s_chunks[tid] = chunks;
+    s_nz[tid] = nz;
+    __syncthreads();
+    for (int o = 1; o < T; o <<= 1) {  // inclusive Hillis-Steele scan
+        const int64_t c = tid >= o ? s_chunks[tid - o] : 0;
+        const int32_t z = tid >= o ? s_nz[tid - o] : 0;
+        __syncthreads();
+        s_chunks[tid] += c;
+        s_nz[tid] += z;
+        __syncthreads();
+    }
+    int64_t cpos = s_chunks[tid] - chunks;
+    int32_t spos = s_nz[tid] - nz;
+    for (int64_t r = lo; r < hi; ++r) {
+        const int64_t add = next[r];
+        if (add <= 0) continue;
+        const int64_t b = rays_total[r], g0 = b >> 2, g1 = (b + add + 3) >> 2;
+        Segment sg;
+        sg.emitter = row_emitter[r];
+        sg.scene = row_scene[r];
+        sg.ray_begin = b;
+        sg.ray_end = b + add;
+        sg.chunk_begin = cpos;
+        seg[spos++] = sg;
+        cpos += (g1 - g0 + chunk_draws - 1) / chunk_draws;
+        rays_total[r] = b + add;
+    }
+    if (tid == T - 1) {
+        *d_nseg = s_nz[T - 1];
+        *d_total = s_chunks[T - 1];
+        *queue = 0ull;
+    }
+}
+
+cudaError_t launch_plan_round(int64_t nrows, const int32_t *row_scene, const int32_t *row_emitter,
+                              int64_t *rays_total, const int64_t *next, Segment *seg, int32_t *d_nseg,
+                              int64_t *d_total, unsigned long long *queue, int chunk_draws, cudaStream_t st)
+{
+    plan_round_kernel<<<1, 1024, 0, st>>>(nrows, row_scene, row_emitter, rays_total, next, seg, d_nseg,
+                                          d_total, queue, chunk_draws);
+    return cudaGetLastError();
+}
+
+// Loop control of the convergence graph: one more round while some row is
+// above the tolerance and fewer than max_rounds rounds ran.
+__global__ void decide_round_kernel(int32_t *flags, int32_t max_rounds, cudaGraphConditionalHandle h)
+{
+    const int32_t rounds = flags[1] + 1;
+    flags[1] = rounds;
+    const bool more = flags[0] > 0 && rounds < max_rounds;
+    flags[0] = 0;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+cudaError_t launch_decide_round(int32_t *flags, int32_t max_rounds, unsigned long long handle,
+                                cudaStream_t st)
+{
+    decide_round_kernel<<<1, 1, 0, st>>>(flags, max_rounds, (cudaGraphConditionalHandle)handle);
+    return cudaGetLastError();
+}
+
 __device__ __forceinline__ void atomic_max_double(double *a, double v)
 {
     // non-negative doubles order like their bit patterns

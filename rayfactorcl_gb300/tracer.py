@@ -128,6 +128,69 @@ class Tracer:
                                           ptr(hits), ptr(F)))
         return rays, hits.astype(np.int64), F
 
+    def refined_count(self) -> int:
+        """Quadric tests re-evaluated in FP64 by the last mixed-precision run."""
+        v = ctypes.c_uint64()
+        self._check(self._L.rf_last_refine_count(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def work_counts(self) -> np.ndarray:
+        """[tests by type x6, cone tests, packets] of the last mixed-precision run."""
+        out = np.zeros(8, np.uint64)
+        self._check(self._L.rf_last_work_counts(self._h, ptr(out)))
+        return out
+
+    def _descs(self, scenes, rays_list):
+        keep, descs = [], (_lib.RfSceneDesc * len(scenes))()
+        for i, (sc, r) in enumerate(zip(scenes, rays_list)):
+            prims = np.ascontiguousarray(sc.primitives, PRIM_DTYPE)
+            rr = np.ascontiguousarray(np.broadcast_to(np.asarray(r, np.int64), (prims.shape[0],)), np.int64)
+            keep += [prims, rr]
+            descs[i].prims = prims.ctypes.data
+            descs[i].n_prims = prims.shape[0]
+            descs[i].rays_per_emitter = rr.ctypes.data
+        return descs, keep
+
+    def _split(self, scenes, flat):
+        out, off = [], 0
+        for sc in scenes:
+            n = sc.primitives.shape[0]
+            out.append(flat[off:off + n * n].reshape(n, n))
+            off += n * n
+        return out
+
+    def trace_batch(self, scenes, rays_list):
+        """One persistent launch over many scenes (mixed precision).  Lists of
+        per-scene tally and F matrices."""
+        descs, keep = self._descs(scenes, rays_list)
+        tot = sum(int(sc.primitives.shape[0]) ** 2 for sc in scenes)
+        hits = np.zeros(tot, np.uint64)
+        F = np.zeros(tot, np.float64)
+        self._check(self._L.rf_trace_batch(self._h, descs, len(scenes), ptr(hits), ptr(F)))
+        del keep
+        return self._split(scenes, hits.astype(np.int64)), self._split(scenes, F)
+
+    def converge_batch(self, scenes, rays_list, tol: float, round_rays: int, max_rounds: int):
+        """Add rays until every row's binomial standard error is <= tol (CUDA-graph
+        loop on the device).  Returns (hits list, F list, rays list, rounds)."""
+        descs, keep = self._descs(scenes, rays_list)
+        tot = sum(int(sc.primitives.shape[0]) ** 2 for sc in scenes)
+        nrows = sum(int(sc.primitives.shape[0]) for sc in scenes)
+        hits = np.zeros(tot, np.uint64)
+        F = np.zeros(tot, np.float64)
+        rays = np.zeros(nrows, np.int64)
+        rounds = ctypes.c_int32()
+        self._check(self._L.rf_converge_batch(self._h, descs, len(scenes), float(tol), int(round_rays),
+                                              int(max_rounds), ptr(hits), ptr(F), ptr(rays),
+                                              ctypes.byref(rounds)))
+        del keep
+        rl, off = [], 0
+        for sc in scenes:
+            n = sc.primitives.shape[0]
+            rl.append(rays[off:off + n].copy())
+            off += n
+        return self._split(scenes, hits.astype(np.int64)), self._split(scenes, F), rl, rounds.value
+
     def check_F(self, F: np.ndarray, areas: np.ndarray | None = None):
         F = np.ascontiguousarray(F, np.float64)
         a = None if areas is None else np.ascontiguousarray(areas, np.float64)

@@ -1,0 +1,155 @@
+"""GPU tests of the batched mixed-precision kernel.
+
+Its nearest hits come from FP32 approximations (FP64 for ill-conditioned
+quadrics) after bounding-sphere culling of coherent ray packets, so rays are
+compared with the FP64 oracle on identical streams and disagreements (grazing
+rays) are counted and bounded; F is compared with the plain kernel, the
+closed forms and the FP64 tracer.
+"""
+import numpy as np
+import pytest
+
+from helpers import binom_sigma, gen_scene, golden_scene
+from oracle import oracle as O
+from rayfactorcl_gb300 import analytic
+from rayfactorcl_gb300.tracer import PREC_EXACT, PREC_FP64, PREC_MIXED, Tracer
+
+pytestmark = pytest.mark.gpu
+
+
+def _tracer(scene, **kw):
+    t = Tracer(**kw)
+    t.set_scene(scene)
+    return t
+
+
+@pytest.mark.parametrize("name", ["gen_mixed64", "input-furnace", "input-W100", "gen_sweep0",
+                                  "input-C122", "input-C14", "input-C47", "input-C109", "gen_enclosure3"])
+def test_mixed_per_ray_vs_fp64_oracle(built_lib, oracle_lib, name):
+    sc = golden_scene(name)
+    p = O.params(compat=0)
+    total = bad = 0
+    emitters = sorted(set([0, sc.n // 2, sc.n - 1]))
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        for e in emitters:
+            got = t.trace_rays(e, 0, 8192)
+            exp = O.trace_rays(sc, p, e, 0, 8192, f64=True)
+            total += got.size
+            bad += int(np.count_nonzero(got != exp))
+    assert bad / total <= 2e-3, (bad, total)
+
+
+def test_mixed_beats_fp32_on_far_offsets(built_lib, oracle_lib):
+    """Unit surfaces 1e4 from the origin, thin annuli, 89.9 degree frusta: the
+    mixed kernel (re-centred, FP64 for ill-conditioned roots) agrees with the
+    FP64 tracer far better than plain FP32."""
+    sc = golden_scene("gen_precision_stress")
+    p = O.params(compat=0)
+    bad_mixed = bad_exact = total = 0
+    with _tracer(sc, precision=PREC_MIXED) as tm:
+        for e in range(sc.n):
+            ref = O.trace_rays(sc, p, e, 0, 4096, f64=True)
+            bad_mixed += int(np.count_nonzero(tm.trace_rays(e, 0, 4096) != ref))
+            bad_exact += int(np.count_nonzero(O.trace_rays(sc, p, e, 0, 4096) != ref))
+            total += ref.size
+    assert bad_mixed / total < 5e-3, (bad_mixed, total)
+    assert bad_mixed < bad_exact, (bad_mixed, bad_exact)
+
+
+def test_mixed_tallies_equal_fp64_statistics(built_lib, oracle_lib):
+    """Same streams: tallies of the mixed kernel differ from the FP64 tracer's only by
+    the few grazing rays, far inside one standard error."""
+    sc = golden_scene("gen_mixed64")
+    rays = np.full(sc.n, 40_000, np.int64)
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        hm, Fm = t.trace(rays)
+        nref = t.refined_count()
+    with _tracer(sc, precision=PREC_FP64) as t:
+        h64, F64 = t.trace(rays)
+    diff = np.abs(hm - h64).sum()
+    assert diff <= 2e-3 * rays.sum(), diff
+    assert np.all(np.abs(Fm - F64) <= binom_sigma(F64, rays[:, None]) + 1e-4)
+    assert nref >= 0
+
+
+def test_enclosure_mixed_analytic(built_lib):
+    sc = gen_scene("gen_enclosure3")
+    n = 50_000_000
+    with _tracer(sc, precision=PREC_MIXED, key1=1) as t:
+        hits, F = t.trace(np.full(3, n))
+    ref = analytic.enclosure3()
+    sig = binom_sigma(ref, n)
+    assert np.all(np.abs(F - ref) <= 5 * sig + 1.5e-3), F - ref
+    assert abs(F[0, 1] - ref[0, 1]) < 5 * sig[0, 1] + 3e-4
+
+
+def test_batch_equals_single_scene_runs(built_lib):
+    """Scene s of a batch draws the streams of scene_id = s; each scene's tallies equal a
+    single-scene mixed run with that scene_id, whatever the other scenes are."""
+    names = ["gen_sweep1", "gen_enclosure3", "gen_mixed64", "gen_sweep2", "input-C47"]
+    scenes = [golden_scene(n) for n in names]
+    rng = np.random.default_rng(3)
+    rays = [rng.integers(0, 30000, sc.n).astype(np.int64) for sc in scenes]
+    with Tracer(precision=PREC_MIXED) as t:
+        hits, F = t.trace_batch(scenes, rays)
+    for s, (sc, r) in enumerate(zip(scenes, rays)):
+        with _tracer(sc, precision=PREC_MIXED, scene_id=s) as t1:
+            h1, F1 = t1.trace(r)
+        assert np.array_equal(hits[s], h1), names[s]
+        nz = r > 0
+        assert np.allclose(F[s][nz], F1[nz])
+        assert np.isnan(F[s][~nz]).all()
+
+
+def test_convergence_loop(built_lib):
+    """The graph-driven loop stops when every row's standard error is <= tol, and its
+    tallies equal one batch trace with the final budgets (streams continue)."""
+    scenes = [golden_scene("gen_enclosure3"), golden_scene("input-C52"), golden_scene("gen_sweep2")]
+    init = [np.full(sc.n, 4096, np.int64) for sc in scenes]
+    tol = 2e-3
+    with Tracer(precision=PREC_MIXED) as t:
+        hits, F, rays, rounds = t.converge_batch(scenes, init, tol=tol, round_rays=20480, max_rounds=64)
+    assert 1 <= rounds < 64
+    for sc, h, f, r in zip(scenes, hits, F, rays):
+        assert np.all(r >= 4096)
+        sig = np.sqrt(f * (1 - f) / r[:, None])
+        assert np.all(sig.max(axis=1) <= tol + 1e-12)
+        # rows stop as soon as they converge: one round fewer would not have sufficed
+        assert np.all((r - 4096) % 20480 == 0)
+    with Tracer(precision=PREC_MIXED) as t:
+        h2, F2 = t.trace_batch(scenes, rays)
+    for a, b in zip(hits, h2):
+        assert np.array_equal(a, b)
+
+
+def test_batch_rejects_bad_input(built_lib):
+    from rayfactorcl_gb300 import _lib
+    sc = golden_scene("input-C47")
+    with Tracer(precision=PREC_MIXED) as t:
+        with pytest.raises(_lib.RfError):
+            t.trace_batch([sc], [np.array([-4, 4])])
+        bad = sc.primitives.copy()
+        bad[0]["type"] = 9
+        with pytest.raises(_lib.RfError) as ei:
+            t.trace_batch([type(sc)(1e6, False, bad, sc.bounding_volumes)], [np.array([4, 4])])
+        assert ei.value.status == 2
+        with pytest.raises(_lib.RfError):
+            t.converge_batch([sc], [np.array([4, 4])], tol=0.0, round_rays=4, max_rounds=2)
+        t.set_scene(golden_scene("input-C52-BV"))
+        with pytest.raises(_lib.RfError) as ei:
+            t.trace([4, 4], use_bv=True)
+        assert ei.value.status == 8
+
+
+def test_mixed_far_offset_self_hits(built_lib, oracle_lib):
+    """A planar emitter never sees itself.  At 1e4 from the origin the FP32 ray origins are
+    1e-3 off the plane and plain FP32 reports self-hits; the re-centred mixed kernel does not."""
+    sc = golden_scene("gen_precision_stress")
+    rays = np.zeros(sc.n, np.int64)
+    rays[:4] = 200_000  # the thin annuli
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        hm, _ = t.trace(rays)
+    with _tracer(sc, precision=PREC_FP64) as t:
+        h64, _ = t.trace(rays)
+    for e in range(4):
+        assert hm[e, e] == 0 and h64[e, e] == 0
