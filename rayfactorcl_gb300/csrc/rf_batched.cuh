@@ -11,13 +11,14 @@
 //      RayFactorGPU.cl:298-443),
 //   2. counting-sorts them by direction cell (octahedral map, 8x8 cells in
 //      Morton order), so that 32 consecutive rays point roughly the same way,
-//   3. lets every warp take packets of 32 sorted rays: the packet's origin
-//      ball and direction cone are reduced across the warp, and a surface is
-//      tested only if the cone can reach the surface's bounding sphere (one
-//      warp-uniform test per packet and surface instead of 32 ray tests),
+//   3. lets its warps take packets of 32 sorted rays from a shared counter;
+//      each lane checks its ray against a surface's bounding sphere (a dozen
+//      FP32 operations) and the warp runs the surface's full test only if
+//      some lane's ray can reach the sphere, so coherent packets skip most
+//      surfaces together,
 //   4. evaluates the surviving tests in FP32; a quadric whose discriminant
-//      B^2 - AC lost more than 12 bits to cancellation is re-evaluated in FP64
-//      (counted), and
+//      B^2 - AC is within 64 rounding errors of zero (or a cone whose A lost
+//      12 bits) is re-evaluated in FP64 (counted), and
 //   5. tallies first hits in a shared-memory row histogram flushed as 64-bit
 //      atomics whenever the (scene, emitter) row changes.
 // Skipping a surface whose bounding sphere no ray of the packet can reach does
@@ -33,14 +34,14 @@ constexpr int kBatchThreads = 256;
 constexpr int kBatchDraws = 2;                                   // draws per thread per chunk
 constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 2048
 constexpr int kCells = 64;                                       // direction cells
-constexpr int kBatchTile = 256;                                  // surfaces per staged tile
-constexpr int kBatchHist = 2048;                                 // rows up to this stay in smem
-constexpr float kCondRel = 1.0f / 4096.0f;                       // 12 bits of cancellation
+constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
+constexpr int kBatchHist = 1024;                                 // rows up to this stay in smem
+constexpr float kCondRel = 64.0f / 8388608.0f;                   // 64 ulps of the terms
+constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
 
 struct BatchSmem {
     float ray[6][kChunkRays];           // sx sy sz cx cy cz, by local ray index
-    float tb[kChunkRays];               // best t, by sorted position
-    int bi[kChunkRays];                 // best surface, by sorted position
+    int bi[kChunkRays];                 // rank in bucket, then best surface by sorted position
     uint16_t perm[kChunkRays];          // sorted position -> local ray index
     uint8_t key[kChunkRays];            // direction cell, kCells = invalid ray
     int cnt[kCells + 2];
@@ -49,6 +50,7 @@ struct BatchSmem {
     int hist[kBatchHist];
     rf_primitive emit;
     int64_t chunk;
+    int next_packet;
 };
 
 // Octahedral cell of a direction, 8x8 cells in Morton order.
@@ -70,83 +72,17 @@ __device__ __forceinline__ int direction_cell(float x, float y, float z)
     return m;
 }
 
-// Bounds of a packet of rays (one per lane; invalid lanes excluded).
-struct Packet {
-    float ox, oy, oz, rho;  // origin ball
-    float ax, ay, az;       // cone axis (unit)
-    float cos_t, sin_t;     // cone half-angle
-    bool cull;              // false: the cone is too wide to cull with
-};
-
-__device__ __forceinline__ float warp_sum(float v)
+// Can the ray (origin s, direction c of length ~1) reach the sphere b (centre,
+// radius)?  Conservative: the radius is widened by 1 % for directions that are
+// not exactly unit and for rounding.
+__device__ __forceinline__ bool ray_may_hit(const Ray<float> &r, const float4 b)
 {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ float warp_max(float v)
-{
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ float warp_min(float v)
-{
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
-__device__ __forceinline__ Packet packet_bounds(const Ray<float> &r, bool valid, int nvalid)
-{
-    Packet pk;
-    const float w = valid ? 1.0f : 0.0f;
-    const float inv_n = 1.0f / (float)nvalid;
-    pk.ox = warp_sum(w * r.sx) * inv_n;
-    pk.oy = warp_sum(w * r.sy) * inv_n;
-    pk.oz = warp_sum(w * r.sz) * inv_n;
-    const float dx = r.sx - pk.ox, dy = r.sy - pk.oy, dz = r.sz - pk.oz;
-    pk.rho = sqrtf(warp_max(valid ? dx * dx + dy * dy + dz * dz : 0.0f));
-    const float ilen = rsqrtf(r.cx * r.cx + r.cy * r.cy + r.cz * r.cz);
-    const float nx = r.cx * ilen, ny = r.cy * ilen, nz = r.cz * ilen;
-    float ax = warp_sum(w * nx), ay = warp_sum(w * ny), az = warp_sum(w * nz);
-    const float al = sqrtf(ax * ax + ay * ay + az * az);
-    pk.cull = al > 1e-3f * (float)nvalid;
-    const float ial = pk.cull ? 1.0f / al : 0.0f;
-    pk.ax = ax * ial;
-    pk.ay = ay * ial;
-    pk.az = az * ial;
-    // widen by 1e-4 for rounding in the normalisation and the dot products
-    const float c = warp_min(valid ? nx * pk.ax + ny * pk.ay + nz * pk.az : 1.0f) - 1e-4f;
-    pk.cull = pk.cull && c > 0.0f;  // cones of 90 degrees or wider are not culled
-    pk.cos_t = c;
-    pk.sin_t = sqrtf(fmaxf(0.0f, 1.0f - c * c));
-    // the butterfly sums may differ in the last bit between lanes: use lane 0's
-    pk.ox = __shfl_sync(0xffffffffu, pk.ox, 0);
-    pk.oy = __shfl_sync(0xffffffffu, pk.oy, 0);
-    pk.oz = __shfl_sync(0xffffffffu, pk.oz, 0);
-    pk.rho = __shfl_sync(0xffffffffu, pk.rho, 0);
-    pk.ax = __shfl_sync(0xffffffffu, pk.ax, 0);
-    pk.ay = __shfl_sync(0xffffffffu, pk.ay, 0);
-    pk.az = __shfl_sync(0xffffffffu, pk.az, 0);
-    pk.cos_t = __shfl_sync(0xffffffffu, pk.cos_t, 0);
-    pk.sin_t = __shfl_sync(0xffffffffu, pk.sin_t, 0);
-    pk.cull = __shfl_sync(0xffffffffu, (int)pk.cull, 0) != 0;
-    return pk;
-}
-
-// Can a ray starting in the packet's origin ball with a direction in its cone
-// reach the sphere (c, r)?  Conservative (a margin of 1e-4 relative).
-__device__ __forceinline__ bool packet_may_hit(const Packet &pk, const float4 s)
-{
-    if (!pk.cull) return true;
-    const float vx = s.x - pk.ox, vy = s.y - pk.oy, vz = s.z - pk.oz;
-    const float L2 = vx * vx + vy * vy + vz * vz;
-    const float R = (s.w + pk.rho) * 1.0001f + 1e-6f + 1e-5f * sqrtf(L2);
-    if (L2 <= R * R) return true;
-    const float va = vx * pk.ax + vy * pk.ay + vz * pk.az;
-    // angle(v, axis) <= theta + beta, sin(beta) = R / |v|, in cosines times |v|
-    return va >= pk.cos_t * sqrtf(L2 - R * R) - pk.sin_t * R;
+    const float ox = b.x - r.sx, oy = b.y - r.sy, oz = b.z - r.sz;
+    const float oc2 = ox * ox + oy * oy + oz * oz;
+    const float rr = b.w * 1.01f + 1e-6f;
+    const float r2 = rr * rr;
+    const float bb = ox * r.cx + oy * r.cy + oz * r.cz;
+    return oc2 <= r2 || (bb > 0.0f && oc2 - bb * bb <= r2);
 }
 
 // Mixed-precision tests: FP32 with hardware approximations; quadrics whose
@@ -159,6 +95,8 @@ __device__ __forceinline__ Ray<double> to_f64(const Ray<float> &w)
     return d;
 }
 
+// B^2 - AC within 64 rounding errors of zero: the sign of the discriminant (hit
+// or miss) and the roots are not resolved in FP32.
 __device__ __forceinline__ bool ill_conditioned(float A, float B, float C)
 {
     const float d = B * B - A * C;
@@ -202,7 +140,8 @@ __device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float>
     const float A = fmaf(o.cx, o.cx, fmaf(o.cy, o.cy, -fdir * fdir));
     const float B = -fmaf(o.sx, o.cx, fmaf(o.sy, o.cy, -fstart * fdir));
     const float C = fmaf(o.sx, o.sx, fmaf(o.sy, o.sy, -fstart * fstart));
-    if (ill_conditioned(A, B, C)) {
+    const float Aterms = o.cx * o.cx + o.cy * o.cy + fdir * fdir;
+    if (ill_conditioned(A, B, C) || fabsf(A) < kCondA * Aterms) {
         ++nref;
         return frustum_f64(h, w, eps);
     }
@@ -309,6 +248,7 @@ __global__ void __launch_bounds__(kBatchThreads) batched_kernel(const TraceParam
             cur_emitter = sg.emitter;
         }
         if (tid <= kCells) S.cnt[tid] = 0;
+        if (tid == 0) S.next_packet = 0;
         __syncthreads();
 
         // 1. emission (draw d = g*blockDim + tid, ray l = 4d + v)
@@ -366,53 +306,41 @@ __global__ void __launch_bounds__(kBatchThreads) batched_kernel(const TraceParam
                 S.perm[S.cnt[S.key[l]] + S.bi[l]] = (uint16_t)l;
             }
         __syncthreads();
-        for (int i = tid; i < kChunkRays; i += blockDim.x) {
-            S.tb[i] = MFast::inf();
-            S.bi[i] = -1;
-        }
-        __syncthreads();
 
-        // 3-4. packets of 32 sorted rays per warp, surfaces tile by tile
-        constexpr int kPackets = kChunkRays / 32 / (kBatchThreads / 32);  // per warp
-        const int ntiles = (si.n + kBatchTile - 1) / kBatchTile;
-        for (int tile = 0; tile < ntiles; ++tile) {
-            const int t0 = tile * kBatchTile;
-            const int cnt = min(kBatchTile, si.n - t0);
-            if (si.n > kBatchTile) {
-                __syncthreads();
-                const float4 *src = reinterpret_cast<const float4 *>(p.tab + si.prim_off + t0);
-                float4 *dst = reinterpret_cast<float4 *>(S.tab);
-                for (int i = tid; i < 4 * cnt; i += blockDim.x) dst[i] = __ldg(src + i);
-                for (int i = tid; i < cnt; i += blockDim.x) S.bs[i] = __ldg(p.bsph + si.prim_off + t0 + i);
-                __syncthreads();
-            }
-#pragma unroll 1
-            for (int k = 0; k < kPackets; ++k) {
-                const int pos = (warp * kPackets + k) * 32 + lane;
-                const int l = S.perm[pos];
-                const bool valid = S.key[l] < kCells;
-                const int nvalid = __popc(__ballot_sync(0xffffffffu, valid));
-                if (nvalid == 0) continue;
+        // 3-4. warps take packets of 32 sorted rays from a shared counter
+        const bool resident = si.n <= kBatchTile;
+        const HitRec *gtab = p.tab + si.prim_off;
+        const float4 *gbs = p.bsph + si.prim_off;
+        for (;;) {
+            int k = 0;
+            if (lane == 0) k = atomicAdd(&S.next_packet, 1);
+            k = __shfl_sync(0xffffffffu, k, 0);
+            if (k >= kChunkRays / 32) break;  // warp-uniform
+            const int pos = k * 32 + lane;
+            const int l = S.perm[pos];
+            const bool valid = S.key[l] < kCells;
+            const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+            int bi = -1;
+            if (vmask) {
+                const int nvalid = __popc(vmask);
                 Ray<float> ray;
                 ray.sx = S.ray[0][l]; ray.sy = S.ray[1][l]; ray.sz = S.ray[2][l];
                 ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
-                const Packet pk = packet_bounds(ray, valid, nvalid);
-                float tb = S.tb[pos];
-                int bi = S.bi[pos];
-                w_cone += cnt;
+                float tb = MFast::inf();
+                w_cone += si.n;
                 ++w_packets;
 #pragma unroll 1
-                for (int jj = 0; jj < cnt; ++jj) {
-                    if (!packet_may_hit(pk, S.bs[jj])) continue;  // warp-uniform
-                    const HitRec h = S.tab[jj];
+                for (int j = 0; j < si.n; ++j) {
+                    const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
+                    if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, bsj))) continue;
+                    const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
                     const int type = __float_as_int(h.aux.x);
                     if ((unsigned)type < 6u) w_tests[type] += nvalid;
                     const float t = hit_mixed(type, h, ray, eps, sc, nref);
-                    if (t < tb) { tb = t; bi = t0 + jj; }
+                    if (t < tb) { tb = t; bi = j; }
                 }
-                S.tb[pos] = tb;
-                S.bi[pos] = bi;
             }
+            S.bi[pos] = bi;
         }
         __syncthreads();
         // 5. tally (or record) by sorted position; all rays of the chunk share one row
