@@ -30,12 +30,12 @@
 
 namespace rf {
 
-constexpr int kBatchThreads = 256;
-constexpr int kBatchDraws = 2;                                   // draws per thread per chunk
+constexpr int kBatchThreads = 512;
+constexpr int kBatchDraws = 1;                                   // draws per thread per chunk
 constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 2048
 constexpr int kCells = 64;                                       // direction cells
 constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
-constexpr int kBatchHist = 1024;                                 // rows up to this stay in smem
+constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
 constexpr float kCondRel = 64.0f / 8388608.0f;                   // 64 ulps of the terms
 constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
 
@@ -45,8 +45,10 @@ struct BatchSmem {
     uint16_t perm[kChunkRays];          // sorted position -> local ray index
     uint8_t key[kChunkRays];            // direction cell, kCells = invalid ray
     int cnt[kCells + 2];
-    HitRec tab[kBatchTile];
+    HitRec tab[kBatchTile];             // cluster order
     float4 bs[kBatchTile];
+    int orig[kBatchTile];
+    Cluster cl[kBatchMaxClusters];
     int hist[kBatchHist];
     rf_primitive emit;
     int64_t chunk;
@@ -187,7 +189,7 @@ __device__ __forceinline__ float hit_mixed(int type, const HitRec &h, const Ray<
 }
 
 template <bool REC>
-__global__ void __launch_bounds__(kBatchThreads) batched_kernel(const TraceParams p)
+__global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TraceParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchSmem &S = *reinterpret_cast<BatchSmem *>(smem_raw);
@@ -234,11 +236,15 @@ __global__ void __launch_bounds__(kBatchThreads) batched_kernel(const TraceParam
                 hist_on = !REC && si.n <= kBatchHist;
                 if (hist_on)
                     for (int i = tid; i < si.n; i += blockDim.x) S.hist[i] = 0;
-                if (si.n <= kBatchTile) {  // resident table
+                if (si.n <= kBatchTile && si.ncl <= kBatchMaxClusters) {  // resident tables
                     const float4 *src = reinterpret_cast<const float4 *>(p.tab + si.prim_off);
                     float4 *dst = reinterpret_cast<float4 *>(S.tab);
                     for (int i = tid; i < 4 * si.n; i += blockDim.x) dst[i] = __ldg(src + i);
-                    for (int i = tid; i < si.n; i += blockDim.x) S.bs[i] = __ldg(p.bsph + si.prim_off + i);
+                    for (int i = tid; i < si.n; i += blockDim.x) {
+                        S.bs[i] = __ldg(p.bsph + si.prim_off + i);
+                        S.orig[i] = __ldg(p.orig + si.prim_off + i);
+                    }
+                    for (int i = tid; i < si.ncl; i += blockDim.x) S.cl[i] = p.clusters[si.cl_off + i];
                 }
                 cur_scene = sg.scene;
             }
@@ -307,10 +313,16 @@ __global__ void __launch_bounds__(kBatchThreads) batched_kernel(const TraceParam
             }
         __syncthreads();
 
-        // 3-4. warps take packets of 32 sorted rays from a shared counter
-        const bool resident = si.n <= kBatchTile;
+        // 3-4. warps take packets of 32 sorted rays from a shared counter and walk
+        // the scene's clusters: a cluster whose sphere no ray of the packet can
+        // reach is skipped with all its members.  Members are visited out of index
+        // order, so equal distances go to the lower surface index, as in
+        // RayFactorGPU.cl:463-467.
+        const bool resident = si.n <= kBatchTile && si.ncl <= kBatchMaxClusters;
         const HitRec *gtab = p.tab + si.prim_off;
         const float4 *gbs = p.bsph + si.prim_off;
+        const int32_t *gorig = p.orig + si.prim_off;
+        const Cluster *gcl = p.clusters + si.cl_off;
         for (;;) {
             int k = 0;
             if (lane == 0) k = atomicAdd(&S.next_packet, 1);
@@ -327,17 +339,24 @@ __global__ void __launch_bounds__(kBatchThreads) batched_kernel(const TraceParam
                 ray.sx = S.ray[0][l]; ray.sy = S.ray[1][l]; ray.sz = S.ray[2][l];
                 ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
                 float tb = MFast::inf();
-                w_cone += si.n;
                 ++w_packets;
 #pragma unroll 1
-                for (int j = 0; j < si.n; ++j) {
-                    const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
-                    if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, bsj))) continue;
-                    const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
-                    const int type = __float_as_int(h.aux.x);
-                    if ((unsigned)type < 6u) w_tests[type] += nvalid;
-                    const float t = hit_mixed(type, h, ray, eps, sc, nref);
-                    if (t < tb) { tb = t; bi = j; }
+                for (int q = 0; q < si.ncl; ++q) {
+                    const Cluster cq = resident ? S.cl[q] : gcl[q];
+                    ++w_cone;
+                    if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, cq.sphere))) continue;
+#pragma unroll 1
+                    for (int j = cq.start; j < cq.start + cq.count; ++j) {
+                        const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
+                        ++w_cone;
+                        if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, bsj))) continue;
+                        const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
+                        const int idx = resident ? S.orig[j] : __ldg(gorig + j);
+                        const int type = __float_as_int(h.aux.x);
+                        if ((unsigned)type < 6u) w_tests[type] += nvalid;
+                        const float t = hit_mixed(type, h, ray, eps, sc, nref);
+                        if (t < tb || (t == tb && bi >= 0 && idx < bi)) { tb = t; bi = idx; }
+                    }
                 }
             }
             S.bi[pos] = bi;
