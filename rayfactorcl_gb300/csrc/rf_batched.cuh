@@ -33,7 +33,7 @@ namespace rf {
 constexpr int kBatchThreads = 512;
 constexpr int kBatchDraws = 1;                                   // draws per thread per chunk
 constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 2048
-constexpr int kCells = 64;                                       // direction cells
+constexpr int kCells = 256;                                      // sort keys: 64 directions x 4 origins
 constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
 constexpr float kCondRel = 64.0f / 8388608.0f;                   // 64 ulps of the terms
@@ -43,7 +43,7 @@ struct BatchSmem {
     float ray[6][kChunkRays];           // sx sy sz cx cy cz, by local ray index
     int bi[kChunkRays];                 // rank in bucket, then best surface by sorted position
     uint16_t perm[kChunkRays];          // sorted position -> local ray index
-    uint8_t key[kChunkRays];            // direction cell, kCells = invalid ray
+    uint16_t key[kChunkRays];           // sort key, kCells = invalid ray
     int cnt[kCells + 2];
     HitRec tab[kBatchTile];             // cluster order
     float4 bs[kBatchTile];
@@ -53,6 +53,7 @@ struct BatchSmem {
     rf_primitive emit;
     int64_t chunk;
     int next_packet;
+    unsigned long long work[8];
 };
 
 // Octahedral cell of a direction, 8x8 cells in Morton order.
@@ -74,17 +75,15 @@ __device__ __forceinline__ int direction_cell(float x, float y, float z)
     return m;
 }
 
-// Can the ray (origin s, direction c of length ~1) reach the sphere b (centre,
-// radius)?  Conservative: the radius is widened by 1 % for directions that are
-// not exactly unit and for rounding.
+// Can the ray (origin s, direction c of length ~1) reach the sphere b?  b.w is
+// the squared radius, already widened on the host by 1 % (directions are unit
+// only to ~1e-3) and for rounding, so the test is conservative.
 __device__ __forceinline__ bool ray_may_hit(const Ray<float> &r, const float4 b)
 {
     const float ox = b.x - r.sx, oy = b.y - r.sy, oz = b.z - r.sz;
     const float oc2 = ox * ox + oy * oy + oz * oz;
-    const float rr = b.w * 1.01f + 1e-6f;
-    const float r2 = rr * rr;
     const float bb = ox * r.cx + oy * r.cy + oz * r.cz;
-    return oc2 <= r2 || (bb > 0.0f && oc2 - bb * bb <= r2);
+    return oc2 <= b.w || (bb > 0.0f && oc2 - bb * bb <= b.w);
 }
 
 // Mixed-precision tests: FP32 with hardware approximations; quadrics whose
@@ -175,15 +174,16 @@ __device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> 
 }
 
 __device__ __forceinline__ float hit_mixed(int type, const HitRec &h, const Ray<float> &w, float eps,
-                                           bool sc, int &nref)
+                                           bool sc, int &nref, uint32_t &c0, uint32_t &c1, uint32_t &c2,
+                                           uint32_t &c3, uint32_t &c4, uint32_t &c5, int nvalid)
 {
     switch (type) {
-    case RF_RECTANGLE: return rectangle_hit<MFast>(h, w, eps);
-    case RF_DISC: return disc_hit<MFast>(h, w, eps);
-    case RF_ANNULUS: return annulus_hit<MFast>(h, w, eps);
-    case RF_CYLINDER: return cylinder_mixed(h, w, eps, nref);
-    case RF_FRUSTUM: return frustum_mixed(h, w, eps, nref);
-    case RF_SPHERE: return sphere_mixed(h, w, eps, sc, nref);
+    case RF_RECTANGLE: c4 += nvalid; return rectangle_hit<MFast>(h, w, eps);
+    case RF_DISC: c5 += nvalid; return disc_hit<MFast>(h, w, eps);
+    case RF_ANNULUS: c3 += nvalid; return annulus_hit<MFast>(h, w, eps);
+    case RF_CYLINDER: c0 += nvalid; return cylinder_mixed(h, w, eps, nref);
+    case RF_FRUSTUM: c1 += nvalid; return frustum_mixed(h, w, eps, nref);
+    case RF_SPHERE: c2 += nvalid; return sphere_mixed(h, w, eps, sc, nref);
     default: return MFast::inf();
     }
 }
@@ -203,7 +203,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
     SceneInfo si{};
     int nref = 0;
     // work counters (warp-uniform, counted by lane 0)
-    unsigned long long w_tests[6] = {0, 0, 0, 0, 0, 0}, w_cone = 0, w_packets = 0;
+    // work counters, 32-bit per chunk, folded into the block's 64-bit counters
+    uint32_t wt0 = 0, wt1 = 0, wt2 = 0, wt3 = 0, wt4 = 0, wt5 = 0, w_cone = 0, w_packets = 0;
+    if (tid < 8) S.work[tid] = 0ull;
     bool hist_on = false;
 
     auto flush = [&]() {
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                     reinterpret_cast<const float *>(p.emit + si.prim_off + sg.emitter)[tid];
             cur_emitter = sg.emitter;
         }
-        if (tid <= kCells) S.cnt[tid] = 0;
+        for (int i = tid; i <= kCells; i += blockDim.x) S.cnt[i] = 0;
         if (tid == 0) S.next_packet = 0;
         __syncthreads();
 
@@ -280,28 +282,41 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                 const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
                 S.ray[0][l] = ray.sx; S.ray[1][l] = ray.sy; S.ray[2][l] = ray.sz;
                 S.ray[3][l] = ray.cx; S.ray[4][l] = ray.cy; S.ray[5][l] = ray.cz;
-                const int key = valid ? direction_cell(ray.cx, ray.cy, ray.cz) : kCells;
-                S.key[l] = (uint8_t)key;
+                // direction cell (Morton) with the emission quadrant of the
+                // surface parameters (r[0], r[1]) as its two low bits
+                const int key = valid ? (direction_cell(ray.cx, ray.cy, ray.cz) << 2) |
+                                            (r[0] >= 0.5f ? 1 : 0) | (r[1] >= 0.5f ? 2 : 0)
+                                      : kCells;
+                S.key[l] = (uint16_t)key;
                 S.bi[l] = atomicAdd(&S.cnt[key], 1);  // rank within the bucket
             }
         }
         __syncthreads();
-        // 2. counting sort: exclusive scan of the kCells+1 bucket sizes (warp 0)
+        // 2. counting sort: exclusive scan of the kCells+1 bucket sizes (warp 0,
+        // kCells/32 consecutive buckets per lane; the invalid bucket goes last)
         if (warp == 0) {
-            const int a = S.cnt[lane], b = S.cnt[32 + lane];
-            int ia = a, ib = b;
+            constexpr int per = kCells / 32;
+            int loc[per], sum = 0;
+#pragma unroll
+            for (int i = 0; i < per; ++i) {
+                loc[i] = S.cnt[lane * per + i];
+                sum += loc[i];
+            }
+            int incl = sum;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const int ta = __shfl_up_sync(0xffffffffu, ia, o);
-                const int tb2 = __shfl_up_sync(0xffffffffu, ib, o);
-                if (lane >= o) { ia += ta; ib += tb2; }
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
             }
-            const int T1 = __shfl_sync(0xffffffffu, ia, 31);
-            const int T2 = __shfl_sync(0xffffffffu, ib, 31);
+            const int total_valid = __shfl_sync(0xffffffffu, incl, 31);
             __syncwarp();
-            S.cnt[lane] = ia - a;
-            S.cnt[32 + lane] = T1 + ib - b;
-            if (lane == 0) S.cnt[kCells] = T1 + T2;
+            int run = incl - sum;
+#pragma unroll
+            for (int i = 0; i < per; ++i) {
+                S.cnt[lane * per + i] = run;
+                run += loc[i];
+            }
+            if (lane == 0) S.cnt[kCells] = total_valid;
         }
         __syncthreads();
 #pragma unroll
@@ -352,15 +367,21 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                         if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, bsj))) continue;
                         const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
                         const int idx = resident ? S.orig[j] : __ldg(gorig + j);
-                        const int type = __float_as_int(h.aux.x);
-                        if ((unsigned)type < 6u) w_tests[type] += nvalid;
-                        const float t = hit_mixed(type, h, ray, eps, sc, nref);
+                        const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, nref, wt0, wt1,
+                                                  wt2, wt3, wt4, wt5, nvalid);
                         if (t < tb || (t == tb && bi >= 0 && idx < bi)) { tb = t; bi = idx; }
                     }
                 }
             }
             S.bi[pos] = bi;
         }
+        if (lane == 0) {
+            const uint32_t wt[8] = {wt0, wt1, wt2, wt3, wt4, wt5, w_cone, w_packets};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (wt[i]) atomicAdd(&S.work[i], (unsigned long long)wt[i]);
+        }
+        wt0 = wt1 = wt2 = wt3 = wt4 = wt5 = w_cone = w_packets = 0;
         __syncthreads();
         // 5. tally (or record) by sorted position; all rays of the chunk share one row
         for (int pos = tid; pos < kChunkRays; pos += blockDim.x) {
@@ -383,13 +404,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
 #pragma unroll
     for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
     if (lane == 0 && tot && p.refined) atomicAdd(p.refined, (unsigned long long)tot);
-    if (lane == 0 && p.work) {
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-            if (w_tests[i]) atomicAdd(p.work + i, w_tests[i]);
-        atomicAdd(p.work + 6, w_cone);
-        atomicAdd(p.work + 7, w_packets);
-    }
+    __syncthreads();
+    if (tid < 8 && p.work && S.work[tid]) atomicAdd(p.work + tid, S.work[tid]);
 }
 
 }  // namespace rf

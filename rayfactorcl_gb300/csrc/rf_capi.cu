@@ -363,6 +363,14 @@ void build_clusters(const float4 *bs, int n, std::vector<int> &order, std::vecto
     }
 }
 
+// The kernel's ray/sphere test takes the squared radius, widened by 1 % for
+// directions that are unit only to ~1e-3 and for FP32 rounding.
+float4 widen_sq(float4 b)
+{
+    const double r = (double)b.w * 1.01 + 1e-6 + 1e-6 * std::sqrt((double)b.x * b.x + (double)b.y * b.y + (double)b.z * b.z);
+    return make_float4(b.x, b.y, b.z, (float)(r * r));
+}
+
 // Mixed-precision tables of one scene.  The world origin moves (in FP64) to the
 // mean of the surfaces' translations, so a scene placed far from the origin keeps
 // its FP32 resolution: m' = m - anchor, invm' = invm o (x + anchor).  Each surface
@@ -441,9 +449,10 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
         build_clusters(bs0.data(), n, order, cl_s);
         for (int i = 0; i < n; ++i) {
             tab[off + i] = tab0[order[i]];
-            bs[off + i] = bs0[order[i]];
+            bs[off + i] = widen_sq(bs0[order[i]]);
             orig[off + i] = order[i];
         }
+        for (Cluster &q : cl_s) q.sphere = widen_sq(q.sphere);
         c->b_info[s].n = n;
         c->b_info[s].prim_off = (int32_t)off;
         c->b_info[s].hits_off = hoff;
