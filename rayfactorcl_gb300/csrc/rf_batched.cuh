@@ -41,14 +41,15 @@ constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost
 
 struct BatchSmem {
     float ray[6][kChunkRays];           // sx sy sz cx cy cz, by local ray index
-    int bi[kChunkRays];                 // rank in bucket, then best surface by sorted position
+    int16_t bi[kChunkRays];             // rank in bucket, then best surface by sorted position
     uint16_t perm[kChunkRays];          // sorted position -> local ray index
     uint16_t key[kChunkRays];           // sort key, kCells = invalid ray
     int cnt[kCells + 2];
     HitRec tab[kBatchTile];             // cluster order
     float4 bs[kBatchTile];
-    int orig[kBatchTile];
-    Cluster cl[kBatchMaxClusters];
+    uint16_t orig[kBatchTile];
+    float4 cls[kBatchMaxClusters];      // cluster spheres
+    uint32_t clr[kBatchMaxClusters];    // cluster ranges: start | count << 16
     int hist[kBatchHist];
     rf_primitive emit;
     int64_t chunk;
@@ -244,9 +245,13 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                     for (int i = tid; i < 4 * si.n; i += blockDim.x) dst[i] = __ldg(src + i);
                     for (int i = tid; i < si.n; i += blockDim.x) {
                         S.bs[i] = __ldg(p.bsph + si.prim_off + i);
-                        S.orig[i] = __ldg(p.orig + si.prim_off + i);
+                        S.orig[i] = (uint16_t)__ldg(p.orig + si.prim_off + i);
                     }
-                    for (int i = tid; i < si.ncl; i += blockDim.x) S.cl[i] = p.clusters[si.cl_off + i];
+                    for (int i = tid; i < si.ncl; i += blockDim.x) {
+                        const Cluster q = p.clusters[si.cl_off + i];
+                        S.cls[i] = q.sphere;
+                        S.clr[i] = (uint32_t)q.start | ((uint32_t)q.count << 16);
+                    }
                 }
                 cur_scene = sg.scene;
             }
@@ -288,7 +293,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                                             (r[0] >= 0.5f ? 1 : 0) | (r[1] >= 0.5f ? 2 : 0)
                                       : kCells;
                 S.key[l] = (uint16_t)key;
-                S.bi[l] = atomicAdd(&S.cnt[key], 1);  // rank within the bucket
+                S.bi[l] = (int16_t)atomicAdd(&S.cnt[key], 1);  // rank within the bucket
             }
         }
         __syncthreads();
@@ -357,23 +362,35 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                 ++w_packets;
 #pragma unroll 1
                 for (int q = 0; q < si.ncl; ++q) {
-                    const Cluster cq = resident ? S.cl[q] : gcl[q];
+                    float4 csph;
+                    int jb, je;
+                    if (resident) {
+                        csph = S.cls[q];
+                        const uint32_t rg = S.clr[q];
+                        jb = (int)(rg & 0xffffu);
+                        je = jb + (int)(rg >> 16);
+                    } else {
+                        const Cluster cq = gcl[q];
+                        csph = cq.sphere;
+                        jb = cq.start;
+                        je = cq.start + cq.count;
+                    }
                     ++w_cone;
-                    if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, cq.sphere))) continue;
+                    if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, csph))) continue;
 #pragma unroll 1
-                    for (int j = cq.start; j < cq.start + cq.count; ++j) {
+                    for (int j = jb; j < je; ++j) {
                         const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
                         ++w_cone;
                         if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, bsj))) continue;
                         const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
-                        const int idx = resident ? S.orig[j] : __ldg(gorig + j);
+                        const int idx = resident ? (int)S.orig[j] : __ldg(gorig + j);
                         const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, nref, wt0, wt1,
                                                   wt2, wt3, wt4, wt5, nvalid);
                         if (t < tb || (t == tb && bi >= 0 && idx < bi)) { tb = t; bi = idx; }
                     }
                 }
             }
-            S.bi[pos] = bi;
+            S.bi[pos] = (int16_t)bi;
         }
         if (lane == 0) {
             const uint32_t wt[8] = {wt0, wt1, wt2, wt3, wt4, wt5, w_cone, w_packets};
