@@ -1,31 +1,29 @@
 // rf_batched.cuh -- the batched mixed-precision persistent tracing kernel.
 //
 // One launch traces any number of independent scenes.  Work items are chunks
-// of kBatchThreads Philox draws (4 rays each) of one (scene, emitter)
-// segment; a persistent grid pulls them from a device queue (an atomic
-// counter), so scenes of 10 and of 400 surfaces load-balance.
+// of kBatchDraws*kBatchThreads Philox draws (4 rays each) of one (scene,
+// emitter) segment; a persistent grid pulls them from a device queue (an
+// atomic counter), so scenes of 10 and of 400 surfaces load-balance.
 //
 // Per chunk a block
 //   1. emits its 2048 rays with FP32 hardware approximations into shared memory
 //      (same streams and emission formulas as the plain kernel,
-//      RayFactorGPU.cl:298-443; directions normalised to unit length),
+//      RayFactorGPU.cl:298-443),
 //   2. counting-sorts them by direction cell (octahedral map, 8x8 cells in
-//      Morton order) and emission quadrant, so that 32 consecutive rays start
-//      and point roughly alike,
-//   3. lets its warps take packets of 32 sorted rays from a shared counter and
-//      walk the scene's bounding-sphere hierarchy together: a node is entered
-//      only if some lane's ray segment [0, best t) reaches its sphere, nearer
-//      child first, so once the packet has hits the far part of the scene is
-//      pruned,
-//   4. evaluates the surviving surface tests in FP32; a quadric whose
-//      discriminant B^2 - AC is within 64 rounding errors of zero (or a cone
-//      whose A lost 12 bits) is re-evaluated in FP64 (counted), and
+//      Morton order), so that 32 consecutive rays point roughly the same way,
+//   3. lets its warps take packets of 32 sorted rays from a shared counter;
+//      each lane checks its ray against a surface's bounding sphere (a dozen
+//      FP32 operations) and the warp runs the surface's full test only if
+//      some lane's ray can reach the sphere, so coherent packets skip most
+//      surfaces together,
+//   4. evaluates the surviving tests in FP32; a quadric whose discriminant
+//      B^2 - AC is within 64 rounding errors of zero (or a cone whose A lost
+//      12 bits) is re-evaluated in FP64 (counted), and
 //   5. tallies first hits in a shared-memory row histogram flushed as 64-bit
 //      atomics whenever the (scene, emitter) row changes.
-// Skipping a node whose sphere no ray of the packet can reach before its
-// current best hit does not change any ray's nearest hit; surfaces are visited
-// out of index order, so equal distances go to the lower index as in
-// RayFactorGPU.cl:463-467.  Only the arithmetic differs from the exact kernel.
+// Skipping a surface whose bounding sphere no ray of the packet can reach does
+// not change any ray's nearest hit; only the arithmetic differs from the
+// exact kernel.
 #pragma once
 
 #include "rf_device.cuh"
@@ -38,7 +36,6 @@ constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 2048
 constexpr int kCells = 256;                                      // sort keys: 64 directions x 4 origins
 constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
-constexpr int kStackDepth = 32;                                  // hierarchy traversal stack per warp
 constexpr float kCondRel = 64.0f / 8388608.0f;                   // 64 ulps of the terms
 constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
 
@@ -48,11 +45,11 @@ struct BatchSmem {
     uint16_t perm[kChunkRays];          // sorted position -> local ray index
     uint16_t key[kChunkRays];           // sort key, kCells = invalid ray
     int cnt[kCells + 2];
-    HitRec tab[kBatchTile];             // hierarchy leaf order
+    HitRec tab[kBatchTile];             // cluster order
+    float4 bs[kBatchTile];
     uint16_t orig[kBatchTile];
-    float4 nsph[kBatchMaxNodes];        // node spheres, squared radius in w
-    uint32_t nlink[kBatchMaxNodes];
-    uint16_t stack[kBatchThreads / 32][kStackDepth];
+    float4 cls[kBatchMaxClusters];      // cluster spheres
+    uint32_t clr[kBatchMaxClusters];    // cluster ranges: start | count << 16
     int hist[kBatchHist];
     rf_primitive emit;
     int64_t chunk;
@@ -79,16 +76,15 @@ __device__ __forceinline__ int direction_cell(float x, float y, float z)
     return m;
 }
 
-// Does the segment s + t c, 0 <= t <= tmax (c unit), come within the sphere b
-// (centre b.xyz, squared radius b.w, widened on the host for rounding)?
-// tmax = -inf (an invalid lane) gives an empty segment.
-__device__ __forceinline__ bool segment_may_hit(const Ray<float> &r, const float4 b, float tmax)
+// Can the ray (origin s, direction c of length ~1) reach the sphere b?  b.w is
+// the squared radius, already widened on the host by 1 % (directions are unit
+// only to ~1e-3) and for rounding, so the test is conservative.
+__device__ __forceinline__ bool ray_may_hit(const Ray<float> &r, const float4 b)
 {
     const float ox = b.x - r.sx, oy = b.y - r.sy, oz = b.z - r.sz;
     const float oc2 = ox * ox + oy * oy + oz * oz;
     const float bb = ox * r.cx + oy * r.cy + oz * r.cz;
-    const float ts = fminf(fmaxf(bb, 0.0f), tmax);  // closest point of the segment
-    return tmax >= 0.0f && oc2 - ts * (2.0f * bb - ts) <= b.w;
+    return oc2 <= b.w || (bb > 0.0f && oc2 - bb * bb <= b.w);
 }
 
 // Mixed-precision tests: FP32 with hardware approximations; quadrics whose
@@ -209,7 +205,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
     int nref = 0;
     // work counters (warp-uniform, counted by lane 0)
     // work counters, 32-bit per chunk, folded into the block's 64-bit counters
-    uint32_t wt0 = 0, wt1 = 0, wt2 = 0, wt3 = 0, wt4 = 0, wt5 = 0, w_node = 0, w_packets = 0;
+    uint32_t wt0 = 0, wt1 = 0, wt2 = 0, wt3 = 0, wt4 = 0, wt5 = 0, w_cone = 0, w_packets = 0;
     if (tid < 8) S.work[tid] = 0ull;
     bool hist_on = false;
 
@@ -243,15 +239,18 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                 hist_on = !REC && si.n <= kBatchHist;
                 if (hist_on)
                     for (int i = tid; i < si.n; i += blockDim.x) S.hist[i] = 0;
-                if (si.n <= kBatchTile && si.nnodes <= kBatchMaxNodes) {  // resident tables
+                if (si.n <= kBatchTile && si.ncl <= kBatchMaxClusters) {  // resident tables
                     const float4 *src = reinterpret_cast<const float4 *>(p.tab + si.prim_off);
                     float4 *dst = reinterpret_cast<float4 *>(S.tab);
                     for (int i = tid; i < 4 * si.n; i += blockDim.x) dst[i] = __ldg(src + i);
-                    for (int i = tid; i < si.n; i += blockDim.x)
+                    for (int i = tid; i < si.n; i += blockDim.x) {
+                        S.bs[i] = __ldg(p.bsph + si.prim_off + i);
                         S.orig[i] = (uint16_t)__ldg(p.orig + si.prim_off + i);
-                    for (int i = tid; i < si.nnodes; i += blockDim.x) {
-                        S.nsph[i] = __ldg(p.node_sph + si.node_off + i);
-                        S.nlink[i] = __ldg(p.node_link + si.node_off + i);
+                    }
+                    for (int i = tid; i < si.ncl; i += blockDim.x) {
+                        const Cluster q = p.clusters[si.cl_off + i];
+                        S.cls[i] = q.sphere;
+                        S.clr[i] = (uint32_t)q.start | ((uint32_t)q.count << 16);
                     }
                 }
                 cur_scene = sg.scene;
@@ -282,9 +281,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                     const int q = (i + v + 1) & 3;
                     r[i] = q == 0 ? uf[0] : (q == 1 ? uf[1] : (q == 2 ? uf[2] : uf[3]));
                 }
-                Ray<float> ray = emit_ray<MFast>(S.emit, r);
-                const float il = MFast::rsqrt(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
-                ray.cx *= il; ray.cy *= il; ray.cz *= il;
+                const Ray<float> ray = emit_ray<MFast>(S.emit, r);
                 const int l = 4 * d + v;
                 const int64_t rid = gid * 4 + v;
                 const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
@@ -336,13 +333,16 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
             }
         __syncthreads();
 
-        // 3-4. warps take packets of 32 sorted rays and walk the hierarchy
-        const bool resident = si.n <= kBatchTile && si.nnodes <= kBatchMaxNodes;
+        // 3-4. warps take packets of 32 sorted rays from a shared counter and walk
+        // the scene's clusters: a cluster whose sphere no ray of the packet can
+        // reach is skipped with all its members.  Members are visited out of index
+        // order, so equal distances go to the lower surface index, as in
+        // RayFactorGPU.cl:463-467.
+        const bool resident = si.n <= kBatchTile && si.ncl <= kBatchMaxClusters;
         const HitRec *gtab = p.tab + si.prim_off;
+        const float4 *gbs = p.bsph + si.prim_off;
         const int32_t *gorig = p.orig + si.prim_off;
-        const float4 *gsph = p.node_sph + si.node_off;
-        const uint32_t *glink = p.node_link + si.node_off;
-        uint16_t *stk = S.stack[warp];
+        const Cluster *gcl = p.clusters + si.cl_off;
         for (;;) {
             int k = 0;
             if (lane == 0) k = atomicAdd(&S.next_packet, 1);
@@ -355,79 +355,50 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
             int bi = -1;
             if (vmask) {
                 const int nvalid = __popc(vmask);
-                const int lead = __ffs(vmask) - 1;
                 Ray<float> ray;
                 ray.sx = S.ray[0][l]; ray.sy = S.ray[1][l]; ray.sz = S.ray[2][l];
                 ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
-                // an invalid lane has t = -inf: an empty segment that never updates
-                float tb = valid ? MFast::inf() : -MFast::inf();
+                float tb = MFast::inf();
                 ++w_packets;
-                int node = 0, sp = 0;
-                ++w_node;
-                bool go = __any_sync(0xffffffffu, segment_may_hit(ray, resident ? S.nsph[0] : __ldg(gsph), tb));
-                while (go) {
-                    const uint32_t lk = resident ? S.nlink[node] : __ldg(glink + node);
-                    bool descended = false;
-                    if (lk & kNodeLeaf) {
-                        const int jb = (int)(lk & 0xffffu), je = jb + (int)((lk >> 16) & 0x7fffu);
 #pragma unroll 1
-                        for (int j = jb; j < je; ++j) {
-                            const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
-                            const int idx = resident ? (int)S.orig[j] : __ldg(gorig + j);
-                            const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, nref, wt0,
-                                                      wt1, wt2, wt3, wt4, wt5, nvalid);
-                            if (valid && (t < tb || (t == tb && bi >= 0 && idx < bi))) { tb = t; bi = idx; }
-                        }
+                for (int q = 0; q < si.ncl; ++q) {
+                    float4 csph;
+                    int jb, je;
+                    if (resident) {
+                        csph = S.cls[q];
+                        const uint32_t rg = S.clr[q];
+                        jb = (int)(rg & 0xffffu);
+                        je = jb + (int)(rg >> 16);
                     } else {
-                        const int a = node + 1, b = (int)(lk & 0xffffu);
-                        const float4 sa = resident ? S.nsph[a] : __ldg(gsph + a);
-                        const float4 sb = resident ? S.nsph[b] : __ldg(gsph + b);
-                        w_node += 2;
-                        const bool pa = __any_sync(0xffffffffu, segment_may_hit(ray, sa, tb));
-                        const bool pb = __any_sync(0xffffffffu, segment_may_hit(ray, sb, tb));
-                        if (pa && pb && sp < kStackDepth) {
-                            // nearer child first, by the lead ray's distance along its direction
-                            const float da = (sa.x - ray.sx) * ray.cx + (sa.y - ray.sy) * ray.cy + (sa.z - ray.sz) * ray.cz;
-                            const float db = (sb.x - ray.sx) * ray.cx + (sb.y - ray.sy) * ray.cy + (sb.z - ray.sz) * ray.cz;
-                            const bool a_first = __shfl_sync(0xffffffffu, da <= db ? 1 : 0, lead) != 0;
-                            if (lane == 0) stk[sp] = (uint16_t)(a_first ? b : a);
-                            __syncwarp();
-                            ++sp;
-                            node = a_first ? a : b;
-                            descended = true;
-                        } else if (pa) {
-                            node = a;
-                            descended = true;
-                        } else if (pb) {
-                            node = b;
-                            descended = true;
-                        }
+                        const Cluster cq = gcl[q];
+                        csph = cq.sphere;
+                        jb = cq.start;
+                        je = cq.start + cq.count;
                     }
-                    if (descended) continue;
-                    // pop until a node still worth entering (the bounds shrank meanwhile)
-                    go = false;
-                    while (sp > 0) {
-                        --sp;
-                        const int cand = stk[sp];
-                        ++w_node;
-                        const float4 sc2 = resident ? S.nsph[cand] : __ldg(gsph + cand);
-                        if (__any_sync(0xffffffffu, segment_may_hit(ray, sc2, tb))) {
-                            node = cand;
-                            go = true;
-                            break;
-                        }
+                    ++w_cone;
+                    if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, csph))) continue;
+#pragma unroll 1
+                    for (int j = jb; j < je; ++j) {
+                        const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
+                        ++w_cone;
+                        if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, bsj))) continue;
+                        const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
+                        const int idx = resident ? (int)S.orig[j] : __ldg(gorig + j);
+                        const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, nref, wt0, wt1,
+                                                  wt2, wt3, wt4, wt5, nvalid);
+                        if (t < tb || (t == tb && bi >= 0 && idx < bi)) { tb = t; bi = idx; }
                     }
                 }
             }
             S.bi[pos] = (int16_t)bi;
         }
         if (lane == 0) {
-            const uint32_t wt[8] = {wt0, wt1, wt2, wt3, wt4, wt5, w_node, w_packets};
+            const uint32_t wt[8] = {wt0, wt1, wt2, wt3, wt4, wt5, w_cone, w_packets};
 #pragma unroll
             for (int i = 0; i < 8; ++i)
                 if (wt[i]) atomicAdd(&S.work[i], (unsigned long long)wt[i]);
         }
-        wt0 = wt1 = wt2 = wt3 = wt4 = wt5 = w_node = w_packets = 0;
+        wt0 = wt1 = wt2 = wt3 = wt4 = wt5 = w_cone = w_packets = 0;
         __syncthreads();
         // 5. tally (or record) by sorted position; all rays of the chunk share one row
         for (int pos = tid; pos < kChunkRays; pos += blockDim.x) {

@@ -29,21 +29,23 @@ struct Segment {
 };
 
 // Per-scene offsets for the batched kernel.  Its surface tables are stored in
-// the leaf order of a bounding-sphere hierarchy (node_off/nnodes locate the
-// scene's nodes) and orig maps a table position back to the surface index.
+// cluster order: cl_off/ncl locate the scene's clusters (groups of up to
+// kClusterSize surfaces with a common bounding sphere), and orig maps a
+// table position back to the surface index.
 struct SceneInfo {
     int32_t n;           // primitives
     int32_t prim_off;    // first record in the concatenated tables
     int64_t hits_off;    // first tally of its n x n matrix
-    int32_t node_off;    // first hierarchy node
-    int32_t nnodes;      // hierarchy nodes
+    int32_t cl_off;      // first cluster
+    int32_t ncl;         // clusters
 };
 
-// Hierarchy node links (depth-first order; an inner node's left child is the
-// next node): leaf -> kNodeLeaf | start | count << 16 (table range), inner ->
-// index of the right child.
-constexpr uint32_t kNodeLeaf = 0x80000000u;
-constexpr int kLeafSize = 2;
+// One cluster: bounding sphere of its members and their table range.
+struct Cluster {
+    float4 sphere;
+    int32_t start, count, pad0, pad1;
+};
+constexpr int kClusterSize = 8;
 
 struct TraceParams {
     const HitRec *tab;              // surface hit records, n (concatenated over scenes)
@@ -67,10 +69,10 @@ struct TraceParams {
     uint32_t scene_id;
     float eps;
     int32_t use_smem_hist;          // 1: shared-memory row histogram, 0: global atomics
+    const float4 *bsph;             // batched kernel: world bounding sphere per surface
     const int64_t *d_total;         // batched kernel: device-resident chunk count (or null)
     const int32_t *d_nseg;          // batched kernel: device-resident segment count (or null)
-    const float4 *node_sph;         // batched kernel: node bounding spheres (squared radius in w)
-    const uint32_t *node_link;      // batched kernel: node links
+    const Cluster *clusters;        // batched kernel: clusters of all scenes
     const int32_t *orig;            // batched kernel: surface index of each table position
     unsigned long long *work;       // batched kernel: [0..5] ray x surface tests by type,
                                     // [6] packet x surface cone tests, [7] packets
@@ -102,7 +104,7 @@ cudaError_t launch_batched(const TraceParams &p, bool rec, int grid, cudaStream_
 int batched_blocks_per_sm(bool rec);
 size_t batched_smem_bytes();
 constexpr int kBatchChunkDraws = 512;   // Philox draws per chunk of the batched kernel
-constexpr int kBatchMaxNodes = 512;     // hierarchy nodes of a scene kept in shared memory
+constexpr int kBatchMaxClusters = 128;  // clusters of a scene kept in shared memory
 
 // FP64 post-processing and probes (rf_kern_post.cu).
 cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,
