@@ -11,11 +11,13 @@
 //      RayFactorGPU.cl:298-443),
 //   2. counting-sorts them by direction cell (octahedral map, 8x8 cells in
 //      Morton order), so that 32 consecutive rays point roughly the same way,
-//   3. lets its warps take packets of 32 sorted rays from a shared counter;
-//      each lane checks its ray against a surface's bounding sphere (a dozen
-//      FP32 operations) and the warp runs the surface's full test only if
-//      some lane's ray can reach the sphere, so coherent packets skip most
-//      surfaces together,
+//   3. lets its warps take packets of 32 sorted rays from a shared counter.
+//      The packet's origin ball and direction cone are reduced across the
+//      warp; then each lane checks the cone against a different surface's
+//      bounding sphere, 32 surfaces per pass, and a ballot gives the packet's
+//      candidate surfaces.  For each candidate (in index order) every lane
+//      checks its own ray against the sphere, and the full test runs only if
+//      some lane's ray can reach it, so coherent packets skip most surfaces,
 //   4. evaluates the surviving tests in FP32; a quadric whose discriminant
 //      B^2 - AC is within 64 rounding errors of zero (or a cone whose A lost
 //      12 bits) is re-evaluated in FP64 (counted), and
@@ -45,16 +47,14 @@ struct BatchSmem {
     uint16_t perm[kChunkRays];          // sorted position -> local ray index
     uint16_t key[kChunkRays];           // sort key, kCells = invalid ray
     int cnt[kCells + 2];
-    HitRec tab[kBatchTile];             // cluster order
-    float4 bs[kBatchTile];
-    uint16_t orig[kBatchTile];
-    float4 cls[kBatchMaxClusters];      // cluster spheres
-    uint32_t clr[kBatchMaxClusters];    // cluster ranges: start | count << 16
+    HitRec tab[kBatchTile];
+    float4 bs[kBatchTile];              // bounding spheres, squared widened radius in w
     int hist[kBatchHist];
     rf_primitive emit;
     int64_t chunk;
     int next_packet;
     unsigned long long work[8];
+    uint32_t wcount[kBatchThreads / 32][8];  // per warp: tests by type, sphere checks, packets
 };
 
 // Octahedral cell of a direction, 8x8 cells in Morton order.
@@ -76,15 +76,84 @@ __device__ __forceinline__ int direction_cell(float x, float y, float z)
     return m;
 }
 
-// Can the ray (origin s, direction c of length ~1) reach the sphere b?  b.w is
-// the squared radius, already widened on the host by 1 % (directions are unit
-// only to ~1e-3) and for rounding, so the test is conservative.
-__device__ __forceinline__ bool ray_may_hit(const Ray<float> &r, const float4 b)
+// Can the ray (origin s, direction c, idd = 1/|c|^2) reach the sphere b?  b.w
+// is the squared radius, widened on the host by 1 % and for rounding.
+__device__ __forceinline__ bool ray_may_hit(const Ray<float> &r, float idd, const float4 b)
 {
     const float ox = b.x - r.sx, oy = b.y - r.sy, oz = b.z - r.sz;
     const float oc2 = ox * ox + oy * oy + oz * oz;
     const float bb = ox * r.cx + oy * r.cy + oz * r.cz;
-    return oc2 <= b.w || (bb > 0.0f && oc2 - bb * bb <= b.w);
+    return oc2 <= b.w || (bb > 0.0f && oc2 - bb * bb * idd <= b.w);
+}
+
+// Bounds of a packet of rays (one per lane; invalid lanes excluded), the same
+// in every lane.
+struct Packet {
+    float ox, oy, oz, rho;  // origin ball
+    float ax, ay, az;       // cone axis (unit)
+    float cos_t, sin_t;     // cone half-angle
+    bool cull;              // false: the cone is too wide to cull with
+};
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return __shfl_sync(0xffffffffu, v, 0);  // butterfly sums may differ in the last bit
+}
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_min(float v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ Packet packet_bounds(const Ray<float> &r, float idd, bool valid, int nvalid)
+{
+    Packet pk;
+    const float w = valid ? 1.0f : 0.0f;
+    const float inv_n = 1.0f / (float)nvalid;
+    pk.ox = warp_sum(w * r.sx) * inv_n;
+    pk.oy = warp_sum(w * r.sy) * inv_n;
+    pk.oz = warp_sum(w * r.sz) * inv_n;
+    const float dx = r.sx - pk.ox, dy = r.sy - pk.oy, dz = r.sz - pk.oz;
+    pk.rho = sqrtf(warp_max(valid ? dx * dx + dy * dy + dz * dz : 0.0f)) * 1.0001f + 1e-6f;
+    const float ilen = sqrtf(idd);
+    const float nx = r.cx * ilen, ny = r.cy * ilen, nz = r.cz * ilen;
+    const float ax = warp_sum(w * nx), ay = warp_sum(w * ny), az = warp_sum(w * nz);
+    const float al = sqrtf(ax * ax + ay * ay + az * az);
+    const bool ok = al > 1e-3f * (float)nvalid;
+    const float ial = ok ? 1.0f / al : 0.0f;
+    pk.ax = ax * ial;
+    pk.ay = ay * ial;
+    pk.az = az * ial;
+    // widened by 1e-4 for rounding in the normalisations and dot products
+    const float c = warp_min(valid ? nx * pk.ax + ny * pk.ay + nz * pk.az : 1.0f) - 1e-4f;
+    pk.cull = ok && c > 0.0f;  // cones of 90 degrees or wider are not culled
+    pk.cos_t = c;
+    pk.sin_t = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+    return pk;
+}
+
+// Can a ray starting in the packet's origin ball with a direction in its cone
+// reach the sphere b (squared radius in w)?  angle(v, axis) <= theta + beta with
+// sin(beta) = R/|v|, compared in cosines times |v|.
+__device__ __forceinline__ bool packet_may_hit(const Packet &pk, const float4 b)
+{
+    if (!pk.cull) return true;
+    const float vx = b.x - pk.ox, vy = b.y - pk.oy, vz = b.z - pk.oz;
+    const float L2 = vx * vx + vy * vy + vz * vz;
+    const float R = sqrtf(b.w) + pk.rho;
+    const float R2 = R * R;
+    if (L2 <= R2) return true;
+    const float va = vx * pk.ax + vy * pk.ay + vz * pk.az;
+    return va >= pk.cos_t * sqrtf(L2 - R2) - pk.sin_t * R;
 }
 
 // Mixed-precision tests: FP32 with hardware approximations; quadrics whose
@@ -175,16 +244,15 @@ __device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> 
 }
 
 __device__ __forceinline__ float hit_mixed(int type, const HitRec &h, const Ray<float> &w, float eps,
-                                           bool sc, int &nref, uint32_t &c0, uint32_t &c1, uint32_t &c2,
-                                           uint32_t &c3, uint32_t &c4, uint32_t &c5, int nvalid)
+                                           bool sc, int &nref)
 {
     switch (type) {
-    case RF_RECTANGLE: c4 += nvalid; return rectangle_hit<MFast>(h, w, eps);
-    case RF_DISC: c5 += nvalid; return disc_hit<MFast>(h, w, eps);
-    case RF_ANNULUS: c3 += nvalid; return annulus_hit<MFast>(h, w, eps);
-    case RF_CYLINDER: c0 += nvalid; return cylinder_mixed(h, w, eps, nref);
-    case RF_FRUSTUM: c1 += nvalid; return frustum_mixed(h, w, eps, nref);
-    case RF_SPHERE: c2 += nvalid; return sphere_mixed(h, w, eps, sc, nref);
+    case RF_RECTANGLE: return rectangle_hit<MFast>(h, w, eps);
+    case RF_DISC: return disc_hit<MFast>(h, w, eps);
+    case RF_ANNULUS: return annulus_hit<MFast>(h, w, eps);
+    case RF_CYLINDER: return cylinder_mixed(h, w, eps, nref);
+    case RF_FRUSTUM: return frustum_mixed(h, w, eps, nref);
+    case RF_SPHERE: return sphere_mixed(h, w, eps, sc, nref);
     default: return MFast::inf();
     }
 }
@@ -204,9 +272,10 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
     SceneInfo si{};
     int nref = 0;
     // work counters (warp-uniform, counted by lane 0)
-    // work counters, 32-bit per chunk, folded into the block's 64-bit counters
-    uint32_t wt0 = 0, wt1 = 0, wt2 = 0, wt3 = 0, wt4 = 0, wt5 = 0, w_cone = 0, w_packets = 0;
+    // work counters: per warp in shared memory (lane 0), folded per chunk into
+    // the block's 64-bit counters
     if (tid < 8) S.work[tid] = 0ull;
+    if (lane < 8) S.wcount[warp][lane] = 0u;
     bool hist_on = false;
 
     auto flush = [&]() {
@@ -239,19 +308,11 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                 hist_on = !REC && si.n <= kBatchHist;
                 if (hist_on)
                     for (int i = tid; i < si.n; i += blockDim.x) S.hist[i] = 0;
-                if (si.n <= kBatchTile && si.ncl <= kBatchMaxClusters) {  // resident tables
+                if (si.n <= kBatchTile) {  // resident tables
                     const float4 *src = reinterpret_cast<const float4 *>(p.tab + si.prim_off);
                     float4 *dst = reinterpret_cast<float4 *>(S.tab);
                     for (int i = tid; i < 4 * si.n; i += blockDim.x) dst[i] = __ldg(src + i);
-                    for (int i = tid; i < si.n; i += blockDim.x) {
-                        S.bs[i] = __ldg(p.bsph + si.prim_off + i);
-                        S.orig[i] = (uint16_t)__ldg(p.orig + si.prim_off + i);
-                    }
-                    for (int i = tid; i < si.ncl; i += blockDim.x) {
-                        const Cluster q = p.clusters[si.cl_off + i];
-                        S.cls[i] = q.sphere;
-                        S.clr[i] = (uint32_t)q.start | ((uint32_t)q.count << 16);
-                    }
+                    for (int i = tid; i < si.n; i += blockDim.x) S.bs[i] = __ldg(p.bsph + si.prim_off + i);
                 }
                 cur_scene = sg.scene;
             }
@@ -333,16 +394,13 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
             }
         __syncthreads();
 
-        // 3-4. warps take packets of 32 sorted rays from a shared counter and walk
-        // the scene's clusters: a cluster whose sphere no ray of the packet can
-        // reach is skipped with all its members.  Members are visited out of index
-        // order, so equal distances go to the lower surface index, as in
-        // RayFactorGPU.cl:463-467.
-        const bool resident = si.n <= kBatchTile && si.ncl <= kBatchMaxClusters;
+        // 3-4. warps take packets of 32 sorted rays; 32 surfaces per pass are
+        // prefiltered against the packet's cone, candidates get per-ray sphere
+        // checks and, if any lane can reach them, the full test (index order, so
+        // ties go to the lower index as in RayFactorGPU.cl:463-467)
+        const bool resident = si.n <= kBatchTile;
         const HitRec *gtab = p.tab + si.prim_off;
         const float4 *gbs = p.bsph + si.prim_off;
-        const int32_t *gorig = p.orig + si.prim_off;
-        const Cluster *gcl = p.clusters + si.cl_off;
         for (;;) {
             int k = 0;
             if (lane == 0) k = atomicAdd(&S.next_packet, 1);
@@ -358,47 +416,38 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                 Ray<float> ray;
                 ray.sx = S.ray[0][l]; ray.sy = S.ray[1][l]; ray.sz = S.ray[2][l];
                 ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
+                const float idd = 1.0f / (ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
+                const Packet pk = packet_bounds(ray, idd, valid, nvalid);
                 float tb = MFast::inf();
-                ++w_packets;
+                if (lane == 0) S.wcount[warp][7] += 1;
 #pragma unroll 1
-                for (int q = 0; q < si.ncl; ++q) {
-                    float4 csph;
-                    int jb, je;
-                    if (resident) {
-                        csph = S.cls[q];
-                        const uint32_t rg = S.clr[q];
-                        jb = (int)(rg & 0xffffu);
-                        je = jb + (int)(rg >> 16);
-                    } else {
-                        const Cluster cq = gcl[q];
-                        csph = cq.sphere;
-                        jb = cq.start;
-                        je = cq.start + cq.count;
-                    }
-                    ++w_cone;
-                    if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, csph))) continue;
-#pragma unroll 1
-                    for (int j = jb; j < je; ++j) {
+                for (int base = 0; base < si.n; base += 32) {
+                    const int js = base + lane;
+                    bool cand = false;
+                    if (js < si.n) cand = packet_may_hit(pk, resident ? S.bs[js] : __ldg(gbs + js));
+                    unsigned cm = __ballot_sync(0xffffffffu, cand);
+                    if (lane == 0) S.wcount[warp][6] += min(32, si.n - base);
+                    while (cm) {
+                        const int j = base + __ffs(cm) - 1;
+                        cm &= cm - 1;
                         const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
-                        ++w_cone;
-                        if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, bsj))) continue;
+                        if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, idd, bsj))) continue;
                         const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
-                        const int idx = resident ? (int)S.orig[j] : __ldg(gorig + j);
-                        const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, nref, wt0, wt1,
-                                                  wt2, wt3, wt4, wt5, nvalid);
-                        if (t < tb || (t == tb && bi >= 0 && idx < bi)) { tb = t; bi = idx; }
+                        const int type = __float_as_int(h.aux.x);
+                        if (lane == 0 && (unsigned)type < 6u) S.wcount[warp][type] += nvalid;
+                        const float t = hit_mixed(type, h, ray, eps, sc, nref);
+                        if (t < tb) { tb = t; bi = j; }
                     }
                 }
             }
             S.bi[pos] = (int16_t)bi;
         }
-        if (lane == 0) {
-            const uint32_t wt[8] = {wt0, wt1, wt2, wt3, wt4, wt5, w_cone, w_packets};
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (wt[i]) atomicAdd(&S.work[i], (unsigned long long)wt[i]);
+        __syncwarp();
+        if (lane < 8) {
+            const uint32_t v = S.wcount[warp][lane];
+            if (v) atomicAdd(&S.work[lane], (unsigned long long)v);
+            S.wcount[warp][lane] = 0u;
         }
-        wt0 = wt1 = wt2 = wt3 = wt4 = wt5 = w_cone = w_packets = 0;
         __syncthreads();
         // 5. tally (or record) by sorted position; all rays of the chunk share one row
         for (int pos = tid; pos < kChunkRays; pos += blockDim.x) {

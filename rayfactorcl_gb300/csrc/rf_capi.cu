@@ -98,7 +98,7 @@ struct rf_ctx {
     int block = 0, gpt = 0, hist = -1;
 
     // batched mixed-precision path: scenes concatenated, re-centred in FP64
-    DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters, b_orig, b_clusters;
+    DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters;
     std::vector<SceneInfo> b_info;
     int64_t b_hits_total = 0;
     bool b_single = false;      // b_* hold the scene of rf_set_scene
@@ -301,68 +301,6 @@ rf_status validate_prims(rf_ctx *c, const rf_primitive *prims, int32_t n, int sc
     return RF_OK;
 }
 
-// Clusters of up to kClusterSize surfaces by recursive median splits of the
-// sphere centres along the longest axis; order receives the surfaces in cluster
-// order, clusters their bounding spheres and ranges.
-void build_clusters(const float4 *bs, int n, std::vector<int> &order, std::vector<Cluster> &clusters)
-{
-    order.resize(n);
-    for (int i = 0; i < n; ++i) order[i] = i;
-    clusters.clear();
-    std::vector<std::pair<int, int>> stack{{0, n}};
-    std::vector<std::pair<int, int>> leaves;
-    while (!stack.empty()) {
-        auto [lo, hi] = stack.back();
-        stack.pop_back();
-        if (hi - lo <= kClusterSize) {
-            leaves.push_back({lo, hi});
-            continue;
-        }
-        float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
-        for (int i = lo; i < hi; ++i) {
-            const float c[3] = {bs[order[i]].x, bs[order[i]].y, bs[order[i]].z};
-            for (int k = 0; k < 3; ++k) {
-                mn[k] = std::min(mn[k], c[k]);
-                mx[k] = std::max(mx[k], c[k]);
-            }
-        }
-        int ax = 0;
-        for (int k = 1; k < 3; ++k)
-            if (mx[k] - mn[k] > mx[ax] - mn[ax]) ax = k;
-        const int mid = lo + (hi - lo) / 2;
-        auto key = [&](int i) { return ax == 0 ? bs[i].x : (ax == 1 ? bs[i].y : bs[i].z); };
-        std::nth_element(order.begin() + lo, order.begin() + mid, order.begin() + hi,
-                         [&](int a, int b) { return key(a) < key(b) || (key(a) == key(b) && a < b); });
-        stack.push_back({mid, hi});
-        stack.push_back({lo, mid});
-    }
-    std::sort(leaves.begin(), leaves.end());
-    for (auto [lo, hi] : leaves) {
-        double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
-        for (int i = lo; i < hi; ++i) {
-            const float4 b = bs[order[i]];
-            const double c[3] = {b.x, b.y, b.z};
-            for (int k = 0; k < 3; ++k) {
-                mn[k] = std::min(mn[k], c[k] - b.w);
-                mx[k] = std::max(mx[k], c[k] + b.w);
-            }
-        }
-        const double C[3] = {0.5 * (mn[0] + mx[0]), 0.5 * (mn[1] + mx[1]), 0.5 * (mn[2] + mx[2])};
-        double r = 0.0;
-        for (int i = lo; i < hi; ++i) {
-            const float4 b = bs[order[i]];
-            const double d = std::sqrt((b.x - C[0]) * (b.x - C[0]) + (b.y - C[1]) * (b.y - C[1]) +
-                                       (b.z - C[2]) * (b.z - C[2]));
-            r = std::max(r, d + b.w);
-        }
-        Cluster cl{};
-        cl.sphere = make_float4((float)C[0], (float)C[1], (float)C[2], (float)(r * (1.0 + 1e-6) + 1e-7));
-        cl.start = lo;
-        cl.count = hi - lo;
-        clusters.push_back(cl);
-    }
-}
-
 // The kernel's ray/sphere test takes the squared radius, widened by 1 % for
 // directions that are unit only to ~1e-3 and for FP32 rounding.
 float4 widen_sq(float4 b)
@@ -434,31 +372,17 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     }
     if (nprim > (1ll << 31) / 4) return fail(c, RF_ERR_OVERFLOW, "too many surfaces in the batch");
     std::vector<rf_primitive> emit(nprim);
-    std::vector<HitRec> tab(nprim), tab0;
-    std::vector<float4> bs(nprim), bs0;
-    std::vector<int32_t> orig(nprim);
-    std::vector<Cluster> cls, cl_s;
-    std::vector<int> order;
+    std::vector<HitRec> tab(nprim);
+    std::vector<float4> bs(nprim);
     c->b_info.resize(ns);
     int64_t off = 0, hoff = 0;
     for (int s = 0; s < ns; ++s) {
         const int n = scenes[s].n_prims;
-        tab0.resize(n);
-        bs0.resize(n);
-        prepare_mixed(scenes[s].prims, n, emit.data() + off, tab0.data(), bs0.data());
-        build_clusters(bs0.data(), n, order, cl_s);
-        for (int i = 0; i < n; ++i) {
-            tab[off + i] = tab0[order[i]];
-            bs[off + i] = widen_sq(bs0[order[i]]);
-            orig[off + i] = order[i];
-        }
-        for (Cluster &q : cl_s) q.sphere = widen_sq(q.sphere);
+        prepare_mixed(scenes[s].prims, n, emit.data() + off, tab.data() + off, bs.data() + off);
+        for (int i = 0; i < n; ++i) bs[off + i] = widen_sq(bs[off + i]);
         c->b_info[s].n = n;
         c->b_info[s].prim_off = (int32_t)off;
         c->b_info[s].hits_off = hoff;
-        c->b_info[s].cl_off = (int32_t)cls.size();
-        c->b_info[s].ncl = (int32_t)cl_s.size();
-        cls.insert(cls.end(), cl_s.begin(), cl_s.end());
         off += n;
         hoff += (int64_t)n * n;
     }
@@ -468,17 +392,14 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     RF_CUDA(c, c->b_emit.ensure(sizeof(rf_primitive) * nprim));
     RF_CUDA(c, c->b_bsph.ensure(sizeof(float4) * nprim));
     RF_CUDA(c, c->b_scenes.ensure(sizeof(SceneInfo) * ns));
-    RF_CUDA(c, c->b_orig.ensure(sizeof(int32_t) * nprim));
-    RF_CUDA(c, c->b_clusters.ensure(sizeof(Cluster) * cls.size()));
+
     RF_CUDA(c, c->b_hits.ensure((size_t)nhits * 8));
     RF_CUDA(c, c->b_counters.ensure(256));
     RF_CUDA(c, cudaMemcpyAsync(c->b_tab.p, tab.data(), sizeof(HitRec) * nprim, cudaMemcpyHostToDevice, c->stream));
     RF_CUDA(c, cudaMemcpyAsync(c->b_emit.p, emit.data(), sizeof(rf_primitive) * nprim, cudaMemcpyHostToDevice, c->stream));
     RF_CUDA(c, cudaMemcpyAsync(c->b_bsph.p, bs.data(), sizeof(float4) * nprim, cudaMemcpyHostToDevice, c->stream));
     RF_CUDA(c, cudaMemcpyAsync(c->b_scenes.p, c->b_info.data(), sizeof(SceneInfo) * ns, cudaMemcpyHostToDevice, c->stream));
-    RF_CUDA(c, cudaMemcpyAsync(c->b_orig.p, orig.data(), sizeof(int32_t) * nprim, cudaMemcpyHostToDevice, c->stream));
-    RF_CUDA(c, cudaMemcpyAsync(c->b_clusters.p, cls.data(), sizeof(Cluster) * cls.size(), cudaMemcpyHostToDevice,
-                               c->stream));
+
     RF_CUDA(c, cudaStreamSynchronize(c->stream));
     c->b_hits_total = nhits;
     return RF_OK;
@@ -503,8 +424,7 @@ TraceParams batch_params(rf_ctx *c)
     p.emit = c->b_emit.as<rf_primitive>();
     p.bsph = c->b_bsph.as<float4>();
     p.scenes = c->b_scenes.as<SceneInfo>();
-    p.orig = c->b_orig.as<int32_t>();
-    p.clusters = c->b_clusters.as<Cluster>();
+
     p.hits = c->b_hits.as<unsigned long long>();
     p.queue = &bc->queue;
     p.refined = &bc->refined;
@@ -642,8 +562,7 @@ void rf_destroy(rf_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (DevBuf *b : {&c->d_tab, &c->d_emit, &c->d_bvtab, &c->d_bvinfo, &c->d_hits, &c->d_seg,
                       &c->d_rays, &c->d_F, &c->d_rec, &c->d_err, &c->d_misc, &c->b_tab, &c->b_emit,
-                      &c->b_bsph, &c->b_scenes, &c->b_hits, &c->b_rows, &c->b_counters, &c->b_orig,
-                      &c->b_clusters})
+                      &c->b_bsph, &c->b_scenes, &c->b_hits, &c->b_rows, &c->b_counters})
         b->release();
     c->h_seg.release();
     c->h_rays.release();

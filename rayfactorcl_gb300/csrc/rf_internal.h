@@ -28,24 +28,12 @@ struct Segment {
     int64_t chunk_begin; // first global chunk index of this segment
 };
 
-// Per-scene offsets for the batched kernel.  Its surface tables are stored in
-// cluster order: cl_off/ncl locate the scene's clusters (groups of up to
-// kClusterSize surfaces with a common bounding sphere), and orig maps a
-// table position back to the surface index.
+// Per-scene offsets for the batched kernel.
 struct SceneInfo {
     int32_t n;           // primitives
     int32_t prim_off;    // first record in the concatenated tables
     int64_t hits_off;    // first tally of its n x n matrix
-    int32_t cl_off;      // first cluster
-    int32_t ncl;         // clusters
 };
-
-// One cluster: bounding sphere of its members and their table range.
-struct Cluster {
-    float4 sphere;
-    int32_t start, count, pad0, pad1;
-};
-constexpr int kClusterSize = 8;
 
 struct TraceParams {
     const HitRec *tab;              // surface hit records, n (concatenated over scenes)
@@ -72,8 +60,6 @@ struct TraceParams {
     const float4 *bsph;             // batched kernel: world bounding sphere per surface
     const int64_t *d_total;         // batched kernel: device-resident chunk count (or null)
     const int32_t *d_nseg;          // batched kernel: device-resident segment count (or null)
-    const Cluster *clusters;        // batched kernel: clusters of all scenes
-    const int32_t *orig;            // batched kernel: surface index of each table position
     unsigned long long *work;       // batched kernel: [0..5] ray x surface tests by type,
                                     // [6] packet x surface cone tests, [7] packets
 };
@@ -104,7 +90,6 @@ cudaError_t launch_batched(const TraceParams &p, bool rec, int grid, cudaStream_
 int batched_blocks_per_sm(bool rec);
 size_t batched_smem_bytes();
 constexpr int kBatchChunkDraws = 512;   // Philox draws per chunk of the batched kernel
-constexpr int kBatchMaxClusters = 128;  // clusters of a scene kept in shared memory
 
 // FP64 post-processing and probes (rf_kern_post.cu).
 cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,
