@@ -38,7 +38,7 @@ constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 2048
 constexpr int kCells = 256;                                      // sort keys: 64 directions x 4 origins
 constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
-constexpr float kCondRel = 64.0f / 8388608.0f;                   // 64 ulps of the terms
+constexpr float kCondRel = 16.0f / 8388608.0f;                   // 16 ulps of the terms
 constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
 
 struct BatchSmem {
@@ -166,7 +166,7 @@ __device__ __forceinline__ Ray<double> to_f64(const Ray<float> &w)
     return d;
 }
 
-// B^2 - AC within 64 rounding errors of zero: the sign of the discriminant (hit
+// B^2 - AC within 16 rounding errors of zero (FP32 evaluates it to a few): the sign of the discriminant (hit
 // or miss) and the roots are not resolved in FP32.
 __device__ __forceinline__ bool ill_conditioned(float A, float B, float C)
 {
@@ -417,26 +417,41 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                 ray.sx = S.ray[0][l]; ray.sy = S.ray[1][l]; ray.sz = S.ray[2][l];
                 ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
                 const float idd = 1.0f / (ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
-                const Packet pk = packet_bounds(ray, idd, valid, nvalid);
                 float tb = MFast::inf();
                 if (lane == 0) S.wcount[warp][7] += 1;
+                // surfaces in blocks of 1024: phase A tests the packet's cone against 32
+                // spheres per pass and keeps one candidate word per lane; phase B walks the
+                // candidates in index order with the per-ray sphere vote and full test
 #pragma unroll 1
-                for (int base = 0; base < si.n; base += 32) {
-                    const int js = base + lane;
-                    bool cand = false;
-                    if (js < si.n) cand = packet_may_hit(pk, resident ? S.bs[js] : __ldg(gbs + js));
-                    unsigned cm = __ballot_sync(0xffffffffu, cand);
-                    if (lane == 0) S.wcount[warp][6] += min(32, si.n - base);
-                    while (cm) {
-                        const int j = base + __ffs(cm) - 1;
-                        cm &= cm - 1;
-                        const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
-                        if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, idd, bsj))) continue;
-                        const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
-                        const int type = __float_as_int(h.aux.x);
-                        if (lane == 0 && (unsigned)type < 6u) S.wcount[warp][type] += nvalid;
-                        const float t = hit_mixed(type, h, ray, eps, sc, nref);
-                        if (t < tb) { tb = t; bi = j; }
+                for (int j0 = 0; j0 < si.n; j0 += 1024) {
+                    const int nwords = min(32, (si.n - j0 + 31) >> 5);
+                    unsigned cmask = 0u;
+                    {
+                        const Packet pk = packet_bounds(ray, idd, valid, nvalid);
+#pragma unroll 1
+                        for (int w = 0; w < nwords; ++w) {
+                            const int js = j0 + (w << 5) + lane;
+                            bool cand = false;
+                            if (js < si.n) cand = packet_may_hit(pk, resident ? S.bs[js] : __ldg(gbs + js));
+                            const unsigned cm = __ballot_sync(0xffffffffu, cand);
+                            if (lane == w) cmask = cm;
+                        }
+                    }
+                    if (lane == 0) S.wcount[warp][6] += min(1024, si.n - j0);
+#pragma unroll 1
+                    for (int w = 0; w < nwords; ++w) {
+                        unsigned cm = __shfl_sync(0xffffffffu, cmask, w);
+                        while (cm) {
+                            const int j = j0 + (w << 5) + __ffs(cm) - 1;
+                            cm &= cm - 1;
+                            const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
+                            if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, idd, bsj))) continue;
+                            const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
+                            const int type = __float_as_int(h.aux.x);
+                            if (lane == 0 && (unsigned)type < 6u) S.wcount[warp][type] += nvalid;
+                            const float t = hit_mixed(type, h, ray, eps, sc, nref);
+                            if (t < tb) { tb = t; bi = j; }
+                        }
                     }
                 }
             }
