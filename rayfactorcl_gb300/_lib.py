@@ -10,7 +10,10 @@ from pathlib import Path
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "librayfactor_gb300.so"
+import os
+
+# RF_LIB_PATH selects another build of the library (for example one installed elsewhere)
+LIB_PATH = Path(os.environ.get("RF_LIB_PATH", str(Path(__file__).resolve().parent / "librayfactor_gb300.so")))
 
 RF_OK = 0
 STATUS = {0: "RF_OK", 1: "RF_ERR_INVALID_ARG", 2: "RF_ERR_BAD_SCENE", 3: "RF_ERR_OOM",
