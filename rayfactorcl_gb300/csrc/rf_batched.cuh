@@ -6,7 +6,7 @@
 // atomic counter), so scenes of 10 and of 400 surfaces load-balance.
 //
 // Per chunk a block
-//   1. emits its 2048 rays with FP32 hardware approximations into shared memory
+//   1. emits its 4096 rays with FP32 hardware approximations into shared memory
 //      (same streams and emission formulas as the plain kernel,
 //      RayFactorGPU.cl:298-443),
 //   2. counting-sorts them by direction cell (octahedral map, 8x8 cells in
@@ -32,14 +32,15 @@
 
 namespace rf {
 
-constexpr int kBatchThreads = 512;
+constexpr int kBatchThreads = 1024;
 constexpr int kBatchDraws = 1;                                   // draws per thread per chunk
-constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 2048
+constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 4096
 constexpr int kCells = 256;                                      // sort keys: 64 directions x 4 origins
 constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
 constexpr float kCondRel = 16.0f / 8388608.0f;                   // 16 ulps of the terms
 constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
+constexpr int kDeferCap = 32;                                    // deferred FP64 tests per packet
 
 struct BatchSmem {
     float ray[6][kChunkRays];           // sx sy sz cx cy cz, by local ray index
@@ -55,6 +56,9 @@ struct BatchSmem {
     int next_packet;
     unsigned long long work[8];
     uint32_t wcount[kBatchThreads / 32][8];  // per warp: tests by type, sphere checks, packets
+    uint32_t dq[kBatchThreads / 32][kDeferCap];  // per warp: deferred tests, surface | lane << 16
+    float dqt[kBatchThreads / 32][kDeferCap];    // their FP64 distances
+    int dqn[kBatchThreads / 32];
 };
 
 // Octahedral cell of a direction, 8x8 cells in Morton order.
@@ -187,22 +191,24 @@ __device__ __noinline__ float sphere_f64(const HitRec &h, const Ray<float> &w, f
     return (float)sphere_hit<MF64>(h, to_f64(w), (double)eps, sc);
 }
 
-__device__ __forceinline__ float cylinder_mixed(const HitRec &h, const Ray<float> &w, float eps, int &nref)
+// The mixed tests set `defer` instead of computing an ill-conditioned root: the
+// caller re-evaluates those tests in FP64 outside its hot loop.
+__device__ __forceinline__ float cylinder_mixed(const HitRec &h, const Ray<float> &w, float eps, bool &defer)
 {
     const Ray<float> o = xfrm_ray<MFast>(h, w);
     const float A = fmaf(o.cx, o.cx, o.cy * o.cy);
     const float B = -fmaf(o.sx, o.cx, o.sy * o.cy);
     const float C = fmaf(o.sx, o.sx, fmaf(o.sy, o.sy, -1.f));
     if (ill_conditioned(A, B, C)) {
-        ++nref;
-        return cylinder_f64(h, w, eps);
+        defer = true;
+        return MFast::inf();
     }
     const float disc = MFast::sqrt(B * B - A * C);
     const float ra = MFast::rcp(A);
     return quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
 }
 
-__device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float> &w, float eps, int &nref)
+__device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float> &w, float eps, bool &defer)
 {
     const Ray<float> o = xfrm_ray<MFast>(h, w);
     const float top = h.aux.y;
@@ -213,8 +219,8 @@ __device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float>
     const float C = fmaf(o.sx, o.sx, fmaf(o.sy, o.sy, -fstart * fstart));
     const float Aterms = o.cx * o.cx + o.cy * o.cy + fdir * fdir;
     if (ill_conditioned(A, B, C) || fabsf(A) < kCondA * Aterms) {
-        ++nref;
-        return frustum_f64(h, w, eps);
+        defer = true;
+        return MFast::inf();
     }
     const float disc = MFast::sqrt(B * B - A * C);
     const float ra = MFast::rcp(A);
@@ -222,7 +228,7 @@ __device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float>
 }
 
 __device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> &w, float eps, bool sc,
-                                              int &nref)
+                                              bool &defer)
 {
     if (sc) return sphere_hit<MFast>(h, w, eps, true);  // reference quirk: no root to refine
     const Ray<float> o = xfrm_ray<MFast>(h, w);
@@ -230,8 +236,8 @@ __device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> 
     const float B = o.cx * o.sx + o.cy * o.sy + o.cz * o.sz;
     const float C = o.sx * o.sx + o.sy * o.sy + o.sz * o.sz - 1.0f;
     if (ill_conditioned(A, B, C)) {
-        ++nref;
-        return sphere_f64(h, w, eps, false);
+        defer = true;
+        return MFast::inf();
     }
     const float d2 = B * B - A * C;
     if (!(d2 >= 0.f)) return MFast::inf();
@@ -244,21 +250,49 @@ __device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> 
 }
 
 __device__ __forceinline__ float hit_mixed(int type, const HitRec &h, const Ray<float> &w, float eps,
-                                           bool sc, int &nref)
+                                           bool sc, bool &defer)
 {
     switch (type) {
     case RF_RECTANGLE: return rectangle_hit<MFast>(h, w, eps);
     case RF_DISC: return disc_hit<MFast>(h, w, eps);
     case RF_ANNULUS: return annulus_hit<MFast>(h, w, eps);
-    case RF_CYLINDER: return cylinder_mixed(h, w, eps, nref);
-    case RF_FRUSTUM: return frustum_mixed(h, w, eps, nref);
-    case RF_SPHERE: return sphere_mixed(h, w, eps, sc, nref);
+    case RF_CYLINDER: return cylinder_mixed(h, w, eps, defer);
+    case RF_FRUSTUM: return frustum_mixed(h, w, eps, defer);
+    case RF_SPHERE: return sphere_mixed(h, w, eps, sc, defer);
     default: return MFast::inf();
     }
 }
 
+// FP64 evaluation of a deferred test (cold path).
+__device__ __noinline__ float hit_f64(const HitRec &h, const Ray<float> &w, float eps, bool sc)
+{
+    switch (__float_as_int(h.aux.x)) {
+    case RF_CYLINDER: return cylinder_f64(h, w, eps);
+    case RF_FRUSTUM: return frustum_f64(h, w, eps);
+    case RF_SPHERE: return sphere_f64(h, w, eps, sc);
+    default: return MFast::inf();
+    }
+}
+
+// Full nearest-hit search for one ray with FP64 for every ill-conditioned
+// quadric (cold path: a packet deferred more tests than its queue holds).
+__device__ __noinline__ int retrace_f64(int n, bool resident, const HitRec *stab, const HitRec *gtab,
+                                        const Ray<float> &ray, float eps, bool sc)
+{
+    float tb = MFast::inf();
+    int bi = -1;
+    for (int j = 0; j < n; ++j) {
+        const HitRec h = resident ? stab[j] : load_rec(gtab, j);
+        bool defer = false;
+        float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
+        if (defer) t = hit_f64(h, ray, eps, sc);
+        if (t < tb) { tb = t; bi = j; }
+    }
+    return bi;
+}
+
 template <bool REC>
-__global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TraceParams p)
+__global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TraceParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchSmem &S = *reinterpret_cast<BatchSmem *>(smem_raw);
@@ -334,7 +368,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
             const int64_t gid = gid0 + d;
             const uint4 u = stream_bits(p.compat, p.key1, sid, sg.emitter, gid);
             const float uf[4] = {u01(u.x), u01(u.y), u01(u.z), u01(u.w)};
-#pragma unroll 1
+#pragma unroll
             for (int v = 0; v < 4; ++v) {
                 float r[4];
 #pragma unroll
@@ -418,7 +452,12 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                 ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
                 const float idd = 1.0f / (ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
                 float tb = MFast::inf();
-                if (lane == 0) S.wcount[warp][7] += 1;
+                bool redo = false;  // this lane's deferred tests overflowed the queue
+                if (lane == 0) {
+                    S.wcount[warp][7] += 1;
+                    S.dqn[warp] = 0;
+                }
+                __syncwarp();
                 // surfaces in blocks of 1024: phase A tests the packet's cone against 32
                 // spheres per pass and keeps one candidate word per lane; phase B walks the
                 // candidates in index order with the per-ray sphere vote and full test
@@ -449,11 +488,43 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_kernel(const TracePa
                             const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
                             const int type = __float_as_int(h.aux.x);
                             if (lane == 0 && (unsigned)type < 6u) S.wcount[warp][type] += nvalid;
-                            const float t = hit_mixed(type, h, ray, eps, sc, nref);
+                            bool defer = false;
+                            const float t = hit_mixed(type, h, ray, eps, sc, defer);
                             if (t < tb) { tb = t; bi = j; }
+                            if (defer && valid) {
+                                const int slot = atomicAdd(&S.dqn[warp], 1);
+                                if (slot < kDeferCap) S.dq[warp][slot] = (uint32_t)j | ((uint32_t)lane << 16);
+                                else redo = true;
+                            }
                         }
                     }
                 }
+                // deferred tests in FP64, spread over the lanes, then merged by their
+                // owners (lower index wins a tie, the tests ran out of index order)
+                __syncwarp();
+                const int nq = min(S.dqn[warp], kDeferCap);
+                if (nq) {
+                    for (int e = lane; e < nq; e += 32) {
+                        const uint32_t q = S.dq[warp][e];
+                        const int lo = S.perm[k * 32 + (int)(q >> 16)];
+                        Ray<float> rq;
+                        rq.sx = S.ray[0][lo]; rq.sy = S.ray[1][lo]; rq.sz = S.ray[2][lo];
+                        rq.cx = S.ray[3][lo]; rq.cy = S.ray[4][lo]; rq.cz = S.ray[5][lo];
+                        const HitRec hq = resident ? S.tab[q & 0xffffu] : load_rec(gtab, (int)(q & 0xffffu));
+                        S.dqt[warp][e] = hit_f64(hq, rq, eps, sc);
+                    }
+                    __syncwarp();
+                    for (int e = 0; e < nq; ++e) {
+                        const uint32_t q = S.dq[warp][e];
+                        if ((int)(q >> 16) == lane) {
+                            const float t = S.dqt[warp][e];
+                            const int j = (int)(q & 0xffffu);
+                            if (t < tb || (t == tb && bi >= 0 && j < bi)) { tb = t; bi = j; }
+                        }
+                    }
+                    nref += (lane == 0) ? nq : 0;
+                }
+                if (redo) bi = retrace_f64(si.n, resident, S.tab, gtab, ray, eps, sc);
             }
             S.bi[pos] = (int16_t)bi;
         }

@@ -89,7 +89,7 @@ template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
 cudaError_t launch_batched(const TraceParams &p, bool rec, int grid, cudaStream_t st);
 int batched_blocks_per_sm(bool rec);
 size_t batched_smem_bytes();
-constexpr int kBatchChunkDraws = 512;   // Philox draws per chunk of the batched kernel
+constexpr int kBatchChunkDraws = 1024;  // Philox draws per chunk of the batched kernel
 
 // FP64 post-processing and probes (rf_kern_post.cu).
 cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,
