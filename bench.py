@@ -331,6 +331,7 @@ def run_ours(args):
         "plain_kernel": plain,
         "speedup_vs_plain": (value / plain["value"]) if plain else None,
         "culled_test_fraction": culled,
+        "work_counts": [int(x) for x in work] if work is not None else None,
         "fp64_refined_tests": refined,
         "f_error": ferr,
         "cpu_baseline": cpu,

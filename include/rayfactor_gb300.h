@@ -203,9 +203,10 @@ rf_status rf_autotune(rf_ctx *ctx, int32_t use_bv, const char *cache_path);
 rf_status rf_last_refine_count(rf_ctx *ctx, uint64_t *refined_tests);
 
 /* Work of the last mixed-precision run: counts[0..5] ray x surface tests
- * performed by surface type (RF_CYLINDER..RF_DISC), counts[6] packet x surface
- * bounding-sphere tests, counts[7] ray packets.  Tests skipped by culling are
- * the all-pairs count minus the sum of counts[0..5]. */
+ * performed by surface type (RF_CYLINDER..RF_DISC), counts[6] candidate
+ * surfaces per packet that passed the packet's cone test (each then checked ray
+ * by ray), counts[7] ray packets (32 rays).  Tests skipped by culling are the
+ * all-pairs count minus the sum of counts[0..5]. */
 rf_status rf_last_work_counts(rf_ctx *ctx, uint64_t *counts);
 
 /* FP32 issue-rate probe: dependent-FMA throughput of the device in FMA/s

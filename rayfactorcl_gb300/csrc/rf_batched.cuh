@@ -40,7 +40,6 @@ constexpr int kBatchTile = 512;                                  // scenes up to
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
 constexpr float kCondRel = 16.0f / 8388608.0f;                   // 16 ulps of the terms
 constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
-constexpr int kDeferCap = 32;                                    // deferred FP64 tests per packet
 
 struct BatchSmem {
     float ray[6][kChunkRays];           // sx sy sz cx cy cz, by local ray index
@@ -56,9 +55,6 @@ struct BatchSmem {
     int next_packet;
     unsigned long long work[8];
     uint32_t wcount[kBatchThreads / 32][8];  // per warp: tests by type, sphere checks, packets
-    uint32_t dq[kBatchThreads / 32][kDeferCap];  // per warp: deferred tests, surface | lane << 16
-    float dqt[kBatchThreads / 32][kDeferCap];    // their FP64 distances
-    int dqn[kBatchThreads / 32];
 };
 
 // Octahedral cell of a direction, 8x8 cells in Morton order.
@@ -452,12 +448,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
                 const float idd = 1.0f / (ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
                 float tb = MFast::inf();
-                bool redo = false;  // this lane's deferred tests overflowed the queue
-                if (lane == 0) {
-                    S.wcount[warp][7] += 1;
-                    S.dqn[warp] = 0;
-                }
-                __syncwarp();
+                int dj = -1, dn = 0;  // deferred FP64 test of this lane (surface, count)
+                if (lane == 0) S.wcount[warp][7] += 1;
                 // surfaces in blocks of 1024: phase A tests the packet's cone against 32
                 // spheres per pass and keeps one candidate word per lane; phase B walks the
                 // candidates in index order with the per-ray sphere vote and full test
@@ -476,7 +468,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             if (lane == w) cmask = cm;
                         }
                     }
-                    if (lane == 0) S.wcount[warp][6] += min(1024, si.n - j0);
+                    // lane w holds word w (0 beyond nwords): candidates of this block
+                    const unsigned ncand = __reduce_add_sync(0xffffffffu, (unsigned)__popc(cmask));
+                    if (lane == 0) S.wcount[warp][6] += ncand;
 #pragma unroll 1
                     for (int w = 0; w < nwords; ++w) {
                         unsigned cm = __shfl_sync(0xffffffffu, cmask, w);
@@ -491,40 +485,21 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             bool defer = false;
                             const float t = hit_mixed(type, h, ray, eps, sc, defer);
                             if (t < tb) { tb = t; bi = j; }
-                            if (defer && valid) {
-                                const int slot = atomicAdd(&S.dqn[warp], 1);
-                                if (slot < kDeferCap) S.dq[warp][slot] = (uint32_t)j | ((uint32_t)lane << 16);
-                                else redo = true;
-                            }
+                            dj = defer ? j : dj;  // predicated, no branch in the hot loop
+                            dn += defer ? 1 : 0;
                         }
                     }
                 }
-                // deferred tests in FP64, spread over the lanes, then merged by their
-                // owners (lower index wins a tie, the tests ran out of index order)
-                __syncwarp();
-                const int nq = min(S.dqn[warp], kDeferCap);
-                if (nq) {
-                    for (int e = lane; e < nq; e += 32) {
-                        const uint32_t q = S.dq[warp][e];
-                        const int lo = S.perm[k * 32 + (int)(q >> 16)];
-                        Ray<float> rq;
-                        rq.sx = S.ray[0][lo]; rq.sy = S.ray[1][lo]; rq.sz = S.ray[2][lo];
-                        rq.cx = S.ray[3][lo]; rq.cy = S.ray[4][lo]; rq.cz = S.ray[5][lo];
-                        const HitRec hq = resident ? S.tab[q & 0xffffu] : load_rec(gtab, (int)(q & 0xffffu));
-                        S.dqt[warp][e] = hit_f64(hq, rq, eps, sc);
-                    }
-                    __syncwarp();
-                    for (int e = 0; e < nq; ++e) {
-                        const uint32_t q = S.dq[warp][e];
-                        if ((int)(q >> 16) == lane) {
-                            const float t = S.dqt[warp][e];
-                            const int j = (int)(q & 0xffffu);
-                            if (t < tb || (t == tb && bi >= 0 && j < bi)) { tb = t; bi = j; }
-                        }
-                    }
-                    nref += (lane == 0) ? nq : 0;
+                // the deferred test in FP64 (lower index wins a tie: it ran out of order);
+                // a lane that deferred more than one test re-traces its ray (cold)
+                if (valid && dn == 1) {
+                    const HitRec hq = resident ? S.tab[dj] : load_rec(gtab, dj);
+                    const float t = hit_f64(hq, ray, eps, sc);
+                    if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
+                } else if (valid && dn > 1) {
+                    bi = retrace_f64(si.n, resident, S.tab, gtab, ray, eps, sc);
                 }
-                if (redo) bi = retrace_f64(si.n, resident, S.tab, gtab, ray, eps, sc);
+                nref += valid ? dn : 0;
             }
             S.bi[pos] = (int16_t)bi;
         }
