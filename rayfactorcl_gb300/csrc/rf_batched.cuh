@@ -287,7 +287,9 @@ __device__ __noinline__ int retrace_f64(int n, bool resident, const HitRec *stab
     return bi;
 }
 
-template <bool REC>
+// RESIDENT: every scene of the launch fits the shared-memory tables
+// (n <= kBatchTile); otherwise surfaces are read through L1.
+template <bool REC, bool RESIDENT>
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TraceParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 hist_on = !REC && si.n <= kBatchHist;
                 if (hist_on)
                     for (int i = tid; i < si.n; i += blockDim.x) S.hist[i] = 0;
-                if (si.n <= kBatchTile) {  // resident tables
+                if (RESIDENT) {  // resident tables
                     const float4 *src = reinterpret_cast<const float4 *>(p.tab + si.prim_off);
                     float4 *dst = reinterpret_cast<float4 *>(S.tab);
                     for (int i = tid; i < 4 * si.n; i += blockDim.x) dst[i] = __ldg(src + i);
@@ -428,7 +430,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
         // prefiltered against the packet's cone, candidates get per-ray sphere
         // checks and, if any lane can reach them, the full test (index order, so
         // ties go to the lower index as in RayFactorGPU.cl:463-467)
-        const bool resident = si.n <= kBatchTile;
+        constexpr bool resident = RESIDENT;
         const HitRec *gtab = p.tab + si.prim_off;
         const float4 *gbs = p.bsph + si.prim_off;
         for (;;) {
@@ -448,7 +450,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
                 const float idd = 1.0f / (ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
                 float tb = MFast::inf();
-                int dj = -1, dn = 0;  // deferred FP64 test of this lane (surface, count)
+                int dj = -1;  // deferred FP64 test of this lane: surface, or -2 for more than one
                 if (lane == 0) S.wcount[warp][7] += 1;
                 // surfaces in blocks of 1024: phase A tests the packet's cone against 32
                 // spheres per pass and keeps one candidate word per lane; phase B walks the
@@ -485,21 +487,21 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             bool defer = false;
                             const float t = hit_mixed(type, h, ray, eps, sc, defer);
                             if (t < tb) { tb = t; bi = j; }
-                            dj = defer ? j : dj;  // predicated, no branch in the hot loop
-                            dn += defer ? 1 : 0;
+                            dj = defer ? (dj == -1 ? j : -2) : dj;  // predicated, no branch
                         }
                     }
                 }
                 // the deferred test in FP64 (lower index wins a tie: it ran out of order);
                 // a lane that deferred more than one test re-traces its ray (cold)
-                if (valid && dn == 1) {
-                    const HitRec hq = resident ? S.tab[dj] : load_rec(gtab, dj);
+                if (valid && dj >= 0) {
+                    const HitRec hq = RESIDENT ? S.tab[dj] : load_rec(gtab, dj);
                     const float t = hit_f64(hq, ray, eps, sc);
                     if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
-                } else if (valid && dn > 1) {
-                    bi = retrace_f64(si.n, resident, S.tab, gtab, ray, eps, sc);
+                    ++nref;
+                } else if (valid && dj == -2) {
+                    bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, ray, eps, sc);
+                    nref += 2;
                 }
-                nref += valid ? dn : 0;
             }
             S.bi[pos] = (int16_t)bi;
         }

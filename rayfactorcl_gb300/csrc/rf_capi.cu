@@ -437,9 +437,16 @@ TraceParams batch_params(rf_ctx *c)
     return p;
 }
 
+bool batch_resident(const rf_ctx *c)
+{
+    for (const SceneInfo &si : c->b_info)
+        if (si.n > batched_tile()) return false;
+    return true;
+}
+
 int batched_grid(rf_ctx *c, bool rec)
 {
-    int bps = batched_blocks_per_sm(rec);
+    int bps = batched_blocks_per_sm(rec, batch_resident(c));
     if (bps <= 0) bps = 1;
     return c->sms * bps;
 }
@@ -467,7 +474,7 @@ rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_
     p.rec_base = rec_base;
     const int grid = (int)std::min<int64_t>(batched_grid(c, rec), total_chunks);
     RF_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    RF_CUDA(c, launch_batched(p, rec, grid, c->stream));
+    RF_CUDA(c, launch_batched(p, rec, batch_resident(c), grid, c->stream));
     RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     c->last_launches = 1;
     c->timed = true;
@@ -969,7 +976,7 @@ rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_sc
         cudaError_t e;
         if ((e = launch_plan_round(nrows, d_sc, d_em, d_total, d_next, c->d_seg.as<Segment>(), &bc->nseg, &bc->total, &bc->queue,
                                    kBatchChunkDraws, c->stream)) != cudaSuccess) return e;
-        if ((e = launch_batched(p, false, grid, c->stream)) != cudaSuccess) return e;
+        if ((e = launch_batched(p, false, batch_resident(c), grid, c->stream)) != cudaSuccess) return e;
         if ((e = launch_converge_step(c->b_hits.as<unsigned long long>(), d_total, d_off, d_len, nrows, nullptr,
                                       tol, d_next, round_rays, &bc->flags[0], c->stream)) != cudaSuccess) return e;
         return launch_decide_round(&bc->flags[0], max_rounds, h, c->stream);

@@ -86,9 +86,10 @@ template <class M> cudaError_t launch_trace(const LaunchCfg &cfg, const TracePar
 template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
 
 // Batched mixed-precision persistent kernel (rf_kern_fast.cu).
-cudaError_t launch_batched(const TraceParams &p, bool rec, int grid, cudaStream_t st);
-int batched_blocks_per_sm(bool rec);
+cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, int grid, cudaStream_t st);
+int batched_blocks_per_sm(bool rec, bool resident);
 size_t batched_smem_bytes();
+int batched_tile();  // scenes with at most this many surfaces use the resident kernel
 constexpr int kBatchChunkDraws = 1024;  // Philox draws per chunk of the batched kernel
 
 // FP64 post-processing and probes (rf_kern_post.cu).

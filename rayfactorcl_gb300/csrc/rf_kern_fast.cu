@@ -12,32 +12,38 @@ static_assert(kBatchThreads * kBatchDraws == kBatchChunkDraws, "chunk size");
 
 size_t batched_smem_bytes() { return sizeof(BatchSmem); }
 
-cudaError_t launch_batched(const TraceParams &p, bool rec, int grid, cudaStream_t st)
+template <bool REC, bool RES>
+static cudaError_t launch_b(const TraceParams &p, int grid, cudaStream_t st)
 {
     const size_t smem = sizeof(BatchSmem);
-    if (rec) {
-        cudaError_t e = cudaFuncSetAttribute(batched_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        batched_kernel<true><<<grid, kBatchThreads, smem, st>>>(p);
-    } else {
-        cudaError_t e = cudaFuncSetAttribute(batched_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        batched_kernel<false><<<grid, kBatchThreads, smem, st>>>(p);
-    }
+    cudaError_t e = cudaFuncSetAttribute(batched_kernel<REC, RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    batched_kernel<REC, RES><<<grid, kBatchThreads, smem, st>>>(p);
     return cudaGetLastError();
 }
 
-int batched_blocks_per_sm(bool rec)
+cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, int grid, cudaStream_t st)
+{
+    if (rec) return resident ? launch_b<true, true>(p, grid, st) : launch_b<true, false>(p, grid, st);
+    return resident ? launch_b<false, true>(p, grid, st) : launch_b<false, false>(p, grid, st);
+}
+
+template <bool REC, bool RES>
+static int occ_b()
 {
     const size_t smem = sizeof(BatchSmem);
     int nb = 0;
-    if (rec) {
-        cudaFuncSetAttribute(batched_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<true>, kBatchThreads, smem);
-    } else {
-        cudaFuncSetAttribute(batched_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<false>, kBatchThreads, smem);
-    }
+    cudaFuncSetAttribute(batched_kernel<REC, RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<REC, RES>, kBatchThreads, smem);
     return nb;
 }
+
+int batched_blocks_per_sm(bool rec, bool resident)
+{
+    if (rec) return resident ? occ_b<true, true>() : occ_b<true, false>();
+    return resident ? occ_b<false, true>() : occ_b<false, false>();
+}
+
+int batched_tile() { return kBatchTile; }
+
 }  // namespace rf
