@@ -35,7 +35,8 @@ namespace rf {
 constexpr int kBatchThreads = 1024;
 constexpr int kBatchDraws = 1;                                   // draws per thread per chunk
 constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 4096
-constexpr int kCells = 256;                                      // sort keys: 64 directions x 4 origins
+constexpr int kDirGrid = 16;                                     // octahedral direction cells per axis
+constexpr int kCells = kDirGrid * kDirGrid * 4;                  // sort keys: 256 directions x 4 origins
 constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
 constexpr float kCondRel = 16.0f / 8388608.0f;                   // 16 ulps of the terms
@@ -57,7 +58,7 @@ struct BatchSmem {
     uint32_t wcount[kBatchThreads / 32][8];  // per warp: tests by type, sphere checks, packets
 };
 
-// Octahedral cell of a direction, 8x8 cells in Morton order.
+// Octahedral cell of a direction, kDirGrid x kDirGrid cells in Morton order.
 __device__ __forceinline__ int direction_cell(float x, float y, float z)
 {
     const float inv = 1.0f / (fabsf(x) + fabsf(y) + fabsf(z) + 1e-30f);
@@ -68,11 +69,12 @@ __device__ __forceinline__ int direction_cell(float x, float y, float z)
         u = uu;
         v = vv;
     }
-    int i = min(7, max(0, (int)((u + 1.0f) * 4.0f)));
-    int j = min(7, max(0, (int)((v + 1.0f) * 4.0f)));
+    constexpr float h = 0.5f * kDirGrid;
+    const int i = min(kDirGrid - 1, max(0, (int)((u + 1.0f) * h)));
+    const int j = min(kDirGrid - 1, max(0, (int)((v + 1.0f) * h)));
     int m = 0;
 #pragma unroll
-    for (int b = 0; b < 3; ++b) m |= (((i >> b) & 1) << (2 * b)) | (((j >> b) & 1) << (2 * b + 1));
+    for (int b = 0; (1 << b) < kDirGrid; ++b) m |= (((i >> b) & 1) << (2 * b)) | (((j >> b) & 1) << (2 * b + 1));
     return m;
 }
 
