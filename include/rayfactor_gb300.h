@@ -213,6 +213,38 @@ rf_status rf_last_work_counts(rf_ctx *ctx, uint64_t *counts);
  * (one FMA counted as one operation), measured with CUDA events. */
 rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s);
 
+/* ---------------------------------------------------------------------------
+ * Tracing without any device allocation.  No counterpart in the reference.
+ *
+ * For hosts that must not let a library allocate GPU memory: an application
+ * that has already reserved the device's memory in its own pool, or a
+ * latency-bound loop that cannot afford the device-wide synchronisation a
+ * cudaMalloc may cause.  The call allocates nothing (no cudaMalloc, cudaFree
+ * or other allocating routine, on the device or the host heap): the caller
+ * passes the scene and budgets in host memory and the tally matrix in device
+ * memory it owns; the prepared surface tables, the segment plan and the
+ * work-queue counters live in one static device array of
+ * RF_NOALLOC_SCRATCH_BYTES per GPU, held from library load until process exit.
+ *
+ * Runs the batched mixed-precision kernel on one scene of at most
+ * RF_NOALLOC_MAX_PRIMS surfaces (more: RF_ERR_OVERFLOW) on the current device,
+ * enqueued on `stream` (a cudaStream_t; NULL = default stream) and returning
+ * without waiting: hits_dev (n x n uint64, zeroed by the call) holds the
+ * tallies once the stream reaches that point.  The tallies equal those of
+ * rf_trace on a context with precision RF_PREC_MIXED, scene_id 0 and the same
+ * compat, key1 and eps.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  Every call reuses the same array and clears what must start at
+ * zero; calls whose GPU work overlaps (other streams, other host threads) race
+ * on it and must be serialised by the caller.
+ * ------------------------------------------------------------------------- */
+#define RF_NOALLOC_MAX_PRIMS 512
+#define RF_NOALLOC_SCRATCH_BYTES (120 * 1024)
+
+rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n_prims,
+                                 const int64_t *rays_per_emitter, uint32_t compat, uint32_t key1,
+                                 float eps, uint64_t *hits_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,7 +33,8 @@ EXPORTS = ("rf_config_default", "rf_create", "rf_destroy", "rf_last_error", "rf_
            "rf_abi_version", "rf_set_scene", "rf_trace", "rf_trace_async", "rf_read_results",
            "rf_last_trace_stats", "rf_stream", "rf_trace_rays", "rf_run_gpurng", "rf_ray_budgets",
            "rf_write_output_txt", "rf_trace_batch", "rf_converge_batch", "rf_check_F",
-           "rf_autotune", "rf_last_refine_count", "rf_last_work_counts", "rf_measure_fp32_peak")
+           "rf_autotune", "rf_last_refine_count", "rf_last_work_counts", "rf_measure_fp32_peak",
+           "rf_trace_mixed_noalloc")
 
 
 class RfConfig(ctypes.Structure):
@@ -92,6 +93,7 @@ def load() -> ctypes.CDLL:
         "rf_last_refine_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
         "rf_last_work_counts": (ctypes.c_int, [P, P]),
         "rf_measure_fp32_peak": (ctypes.c_int, [I32, ctypes.POINTER(ctypes.c_double)]),
+        "rf_trace_mixed_noalloc": (ctypes.c_int, [P, I32, P, U32, U32, ctypes.c_float, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -30,6 +30,7 @@ UNITS = {
     "rf_kern_fast.cu": [],
     "rf_kern_post.cu": [],
     "rf_capi.cu": [],
+    "rf_noalloc.cu": [],
 }
 HEADERS = ["rf_internal.h", "rf_device.cuh", "rf_trace_kernels.cuh", "rf_batched.cuh"]
 

@@ -357,6 +357,18 @@ void prepare_mixed(const rf_primitive *prims, int n, rf_primitive *emit, HitRec 
     }
 }
 
+}  // namespace
+
+// Mixed-precision tables of one scene as the batched kernel reads them
+// (re-centred transforms, hit records, bounding spheres with squared radius).
+void rf::prepare_mixed_tables(const rf_primitive *prims, int n, rf_primitive *emit, HitRec *tab, float4 *bs)
+{
+    prepare_mixed(prims, n, emit, tab, bs);
+    for (int i = 0; i < n; ++i) bs[i] = widen_sq(bs[i]);
+}
+
+namespace {
+
 // Upload the scenes of a batch (one scene for rf_set_scene in MIXED mode).
 rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with_budgets)
 {

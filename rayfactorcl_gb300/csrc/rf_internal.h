@@ -92,6 +92,9 @@ size_t batched_smem_bytes();
 int batched_tile();  // scenes with at most this many surfaces use the resident kernel
 constexpr int kBatchChunkDraws = 1024;  // Philox draws per chunk of the batched kernel
 
+// Host preparation of one scene for the batched kernel (rf_capi.cu).
+void prepare_mixed_tables(const rf_primitive *prims, int n, rf_primitive *emit, HitRec *tab, float4 *bs);
+
 // FP64 post-processing and probes (rf_kern_post.cu).
 cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,
                                     double *F, cudaStream_t st);
