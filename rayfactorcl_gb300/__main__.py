@@ -1,0 +1,52 @@
+"""Command line: the reference program's main() (RayFactorCL/main.cpp:275-284) on the GPU.
+
+    python -m rayfactorcl_gb300 [input.xml] [-o output.txt] [--compat] [--precision exact]
+
+Reads the scene (Scene::readScene, Scene.cpp:24-52), runs runCL_GPURNG with
+n_samples = globalRayDensity (main.cpp:281) and writes the view-factor matrix in
+the reference's output.txt format (main.cpp:236-249).
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+import time
+
+from . import _lib
+from .scene import read_scene
+from .tracer import PREC_EXACT, PREC_FAST, PREC_FP64, PREC_MIXED, run_cl_gpurng
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(prog="python -m rayfactorcl_gb300",
+                                 description="Monte Carlo view factors of a RayFactorCL scene on the GPU")
+    ap.add_argument("input", nargs="?", default="input.xml")
+    ap.add_argument("-o", "--output", default="output.txt")
+    ap.add_argument("--compat", action="store_true",
+                    help="reproduce the reference run for run, including its known quirks")
+    ap.add_argument("--precision", default="exact", choices=["exact", "fast", "mixed", "fp64"])
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args(argv)
+    prec = {"exact": PREC_EXACT, "fast": PREC_FAST, "mixed": PREC_MIXED, "fp64": PREC_FP64}[args.precision]
+    try:
+        scene = read_scene(args.input)
+    except (OSError, ValueError) as e:
+        print(f"Failed to load file \"{args.input}\": {e}", file=sys.stderr)
+        return 1
+    print("=========== RayFactor GB300 =============")
+    print(f"Number of objects : {scene.n}")
+    t0 = time.perf_counter()
+    try:
+        rays, hits, F = run_cl_gpurng(int(scene.global_ray_density), scene, output=args.output,
+                                      precision=prec, device=args.device,
+                                      compat=_lib.COMPAT_ALL if args.compat else 0)
+    except _lib.RfError as e:
+        print(f"rayfactor_gb300: {e}", file=sys.stderr)
+        return 1
+    dt = time.perf_counter() - t0
+    print(f"Rays traced : {int(rays.sum())} in {dt:.3f} s -> {args.output}")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

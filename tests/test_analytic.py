@@ -1,0 +1,216 @@
+"""Closed-form view factors against FP64 quadrature of the view-factor integral,
+and the CPU oracle against the closed forms on the reference's sample scenes."""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import golden_scene, gen_scene
+from oracle import oracle as O
+from rayfactorcl_gb300 import analytic
+
+
+def _gl(n, a, b):
+    x, w = np.polynomial.legendre.leggauss(n)
+    return 0.5 * (b - a) * x + 0.5 * (b + a), 0.5 * (b - a) * w
+
+
+def quad_coaxial_discs(r1, r2, h, n=48):
+    """(1/A1) int int h^2 / (pi s^4) dA2 dA1 over two parallel coaxial discs."""
+    p1, w1 = _gl(n, 0, r1)
+    p2, w2 = _gl(n, 0, r2)
+    ph, wp = _gl(n, 0, 2 * math.pi)
+    P1, P2, PH = np.meshgrid(p1, p2, ph, indexing="ij")
+    W = w1[:, None, None] * w2[None, :, None] * wp[None, None, :]
+    s2 = h * h + P1 ** 2 + P2 ** 2 - 2 * P1 * P2 * np.cos(PH)
+    val = (W * 2 * math.pi * P1 * P2 * h * h / (math.pi * s2 ** 2)).sum()
+    return val / (math.pi * r1 * r1)
+
+
+def quad_perpendicular(w, h, l, n=200):
+    """Rectangle y in [0,w] (plane z=0) to rectangle z in [0,h] (plane y=0), common
+    edge x in [0,l].  The two integrals along the edge are done in closed form,
+    int_0^l int_0^l dx1 dx2 / ((x1-x2)^2 + a^2)^2 = 2 int_0^l (l-u) / (u^2+a^2)^2 du,
+    and the rest by Gauss-Legendre with y = w u^2, z = h v^2 near the edge."""
+    u, wu = _gl(n, 0, 1)
+    U, V = np.meshgrid(u, u, indexing="ij")
+    W = wu[:, None] * wu[None, :]
+    Y, Z = w * U ** 2, h * V ** 2
+    jac = (2 * w * U) * (2 * h * V)
+    a2 = Y ** 2 + Z ** 2
+    a = np.sqrt(a2)
+    inner = l * (l / (2 * a2 * (l * l + a2)) + np.arctan(l / a) / (2 * a2 * a)) \
+        - (1.0 / (2 * a2) - 1.0 / (2 * (l * l + a2)))
+    val = (W * jac * Y * Z * 2 * inner / math.pi).sum()
+    return val / (w * l)
+
+
+def quad_sphere_rect_corner(a, b, h, n=96):
+    """Sphere centre at height h above the corner (0,0) of [0,a]x[0,b]: (1/4pi) int h/d^3 dA."""
+    x, wx = _gl(n, 0, a)
+    y, wy = _gl(n, 0, b)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    d2 = X ** 2 + Y ** 2 + h * h
+    return (wx[:, None] * wy[None, :] * h / d2 ** 1.5).sum() / (4 * math.pi)
+
+
+def quad_sphere_disc(a, h, n=200):
+    r, w = _gl(n, 0, a)
+    return (w * 2 * math.pi * r * h / (r * r + h * h) ** 1.5).sum() / (4 * math.pi)
+
+
+@pytest.mark.parametrize("r1,r2,h", [(0.5, 0.5, 1.0), (1.0, 2.0, 1.0), (1.0, 0.3, 2.5), (2.0, 2.0, 0.5)])
+def test_coaxial_discs(r1, r2, h):
+    assert abs(analytic.coaxial_discs(r1, r2, h) - quad_coaxial_discs(r1, r2, h)) < 2e-6
+
+
+def test_ring_identities():
+    f = analytic.disc_to_ring(1.0, 1.0, 2.0, 1.0)
+    assert abs(f - (quad_coaxial_discs(1, 2, 1) - quad_coaxial_discs(1, 1, 1))) < 3e-6
+    # a ring whose inner radius tends to 0 is a disc
+    assert abs(analytic.ring_to_ring(0.0, 1.0, 0.0, 2.0, 1.0) - analytic.coaxial_discs(1, 2, 1)) < 1e-12
+
+
+@pytest.mark.parametrize("w,h,l", [(1.0, 1.0, 1.0), (2.0, 1.0, 1.0), (0.5, 2.0, 3.0)])
+def test_perpendicular_rectangles(w, h, l):
+    assert abs(analytic.perpendicular_rectangles(w, h, l) - quad_perpendicular(w, h, l)) < 2e-4
+    assert abs(analytic.perpendicular_rectangles(1, 1, 1) - 0.20004) < 1e-4
+
+
+@pytest.mark.parametrize("a,b,h", [(2.0, 2.0, 1.5), (1.0, 3.0, 0.7)])
+def test_sphere_rectangle(a, b, h):
+    assert abs(analytic.sphere_to_rectangle_corner(a, b, h) - quad_sphere_rect_corner(a, b, h)) < 1e-6
+
+
+def test_sphere_disc():
+    assert abs(analytic.sphere_to_coaxial_disc(1.0, 2.0) - quad_sphere_disc(1.0, 2.0)) < 1e-6
+
+
+def test_enclosure_rows_sum_to_one():
+    F = analytic.enclosure3()
+    assert np.allclose(F.sum(axis=1), 1.0)
+    a = np.array([math.pi * 0.25, math.pi * 0.25, math.pi])
+    assert np.allclose(a[:, None] * F, (a[:, None] * F).T)
+
+
+# --- the CPU oracle on the sample geometries against the closed forms ------------
+N_RAYS = 1_000_000
+BIAS = 1.5e-3  # EPS = 1e-3 (RayFactorGPU.cl:7) drops hits closer than 1e-3 to the origin
+
+
+def _F(name, compat=0, f64=False):
+    sc = golden_scene(name) if not name.startswith("gen_") else gen_scene(name)
+    p = O.params(compat=compat, key1=7)
+    hits = O.tally(sc, p, np.full(sc.n, N_RAYS), f64=f64)
+    return hits / N_RAYS
+
+
+def _sig(f):
+    return math.sqrt(max(f * (1 - f), 1e-12) / N_RAYS)
+
+
+@pytest.mark.parametrize("f64", [False, True])
+def test_oracle_C47_disc_to_annulus(oracle_lib, f64):
+    """input-C47.xml: unit disc at z=0, annulus 1..2 at z=1 facing it."""
+    F = _F("input-C47", f64=f64)
+    ref = analytic.disc_to_ring(1.0, 1.0, 2.0, 1.0)
+    assert abs(F[0, 1] - ref) < 5 * _sig(ref) + BIAS
+    assert F[0, 0] == 0 and F[1, 1] == 0
+
+
+def test_oracle_C52_ring_to_ring(oracle_lib):
+    """input-C52.xml: ring 0.5..1 at z=1 facing a coaxial ring 1.5..2 at z=0."""
+    sc = golden_scene("input-C52")
+    F = _F("input-C52")
+    # which ring is which from the tables: util1/util2 are squared radii
+    r = [(math.sqrt(float(p["util1"])), math.sqrt(float(p["util2"]))) for p in sc.primitives]
+    ref01 = analytic.ring_to_ring(r[0][0], r[0][1], r[1][0], r[1][1], 1.0)
+    assert abs(F[0, 1] - ref01) < 5 * _sig(ref01) + BIAS
+
+
+def test_oracle_C14_perpendicular_squares(oracle_lib):
+    F = _F("input-C14")
+    ref = analytic.perpendicular_rectangles(2.0, 2.0, 2.0)
+    for i, j in ((0, 1), (1, 0)):
+        assert abs(F[i, j] - ref) < 5 * _sig(ref) + BIAS
+
+
+def test_oracle_C122_sphere_to_rectangle(oracle_lib):
+    """Sphere (r=1) centred above the corner (1,1) of the square [-1,1]^2 at h=1.5."""
+    F = _F("input-C122")
+    ref = analytic.sphere_to_rectangle_corner(2.0, 2.0, 1.5)
+    assert abs(F[0, 1] - ref) < 5 * _sig(ref) + 2e-4
+    assert F[0, 0] == 0
+
+
+def test_oracle_C109_cone_enclosure(oracle_lib):
+    """input-C109.xml: inward cone (apex up) closed by the unit disc at its base."""
+    F = _F("input-C109")
+    assert abs(F[1, 0] - 1.0) < BIAS + 1e-3           # disc sees only the cone
+    assert abs(F[0, 1] - 1 / math.sqrt(2)) < 5 * _sig(0.7) + BIAS
+
+
+def test_oracle_enclosure_summation_and_reciprocity(oracle_lib):
+    F = _F("gen_enclosure3")
+    ref = analytic.enclosure3()
+    assert np.all(np.abs(F - ref) < 5 * np.vectorize(_sig)(ref) + BIAS)
+    assert np.all(np.abs(F.sum(axis=1) - 1) < 2.5e-3)
+
+
+def test_oracle_compat_sphere_quirk(oracle_lib):
+    """RayFactorGPU.cl:272-288 uses the discriminant without its square root: hit or miss
+    is unchanged (same sign) but the sphere's distance is wrong, so a sphere loses or wins
+    against other surfaces it should not.  Every changed ray involves a sphere."""
+    sc = golden_scene("gen_mixed64")
+    types = sc.primitives["type"]
+    differ = 0
+    for e in (0, 10, 30, 50):
+        q = O.trace_rays(sc, O.params(compat=O.COMPAT_SPHERE), e, 0, 50000)
+        f = O.trace_rays(sc, O.params(compat=0), e, 0, 50000)
+        d = np.nonzero(q != f)[0]
+        differ += d.size
+        for i in d:
+            assert (q[i] >= 0 and types[q[i]] == 2) or (f[i] >= 0 and types[f[i]] == 2)
+    assert differ > 0
+    # C122: the fixed sphere satisfies reciprocity with the closed form
+    F_fix = _F("input-C122", compat=0)
+    ref = analytic.sphere_to_rectangle_corner(2.0, 2.0, 1.5)
+    a_s, a_r = 4 * math.pi, 4.0
+    assert abs(F_fix[1, 0] - a_s * ref / a_r) < 5 * _sig(F_fix[1, 0]) + 2e-3
+
+
+def test_oracle_fp32_fp64_agree(oracle_lib):
+    sc = golden_scene("gen_mixed64")
+    p = O.params(compat=0)
+    bad = total = 0
+    for e in (0, 20, 40, 63):
+        a = O.trace_rays(sc, p, e, 0, 20000)
+        b = O.trace_rays(sc, p, e, 0, 20000, f64=True)
+        bad += int(np.count_nonzero(a != b))
+        total += a.size
+    assert bad / total < 1e-3
+
+
+def test_oracle_bv_stale_quirk(oracle_lib):
+    """BV 0 (checked immediately) holds a far disc; BV 1 (plain) a nearer one: with the
+    reference's stale index (RayFactorGPU.cl:596-619) the far disc keeps the hit."""
+    from rayfactorcl_gb300.scene import parse_scene_xml
+    xml = """<?xml version="1.0" ?><project><settings><globalRayDensity value="1000" />
+    <useBoundingVolumes value="true" /></settings><geometry>
+      <bv type="disc" intermediateCheck="true"><scale x="50" y="50" z="1" />
+        <translation x="0" y="0" z="2" /><children><primitive type="disc">
+          <scale x="50" y="50" z="1" /><translation x="0" y="0" z="2" /></primitive>
+          <primitive type="disc"><scale x="0.5" y="0.5" z="1" /></primitive></children></bv>
+      <bv type="disc"><scale x="50" y="50" z="1" /><translation x="0" y="0" z="1" />
+        <children><primitive type="disc"><scale x="50" y="50" z="1" />
+          <translation x="0" y="0" z="1" /></primitive></children></bv>
+    </geometry></project>"""
+    sc = parse_scene_xml(xml)
+    assert sc.n == 3 and sc.bounding_volumes.shape[0] == 2
+    rays = np.array([0, 20000, 0])
+    stale = O.tally(sc, O.params(compat=O.COMPAT_BV_STALE, use_bv=True), rays)
+    fixed = O.tally(sc, O.params(compat=0, use_bv=True), rays)
+    # rays steep enough to meet both discs: the far disc keeps the hit with the quirk; only
+    # near-horizontal rays that miss the upper disc's rim reach the lower one
+    assert stale[1, 0] > 0.99 * rays[1] and stale[1, 2] < 0.01 * rays[1]
+    assert fixed[1, 2] > 0.99 * rays[1] and fixed[1, 0] == 0      # the nearer plain BV wins

@@ -1,0 +1,191 @@
+"""The C ABI on the CPU: the library loads and exports everything the header
+declares, the header compiles as C and C++ with the reference's struct sizes, the
+integration shim compiles against the reference's own Scene.h, and the host-side
+rules (budgets, output format, validation) behave as the reference does."""
+import ctypes
+import os
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import GEN_NAMES, SAMPLE_NAMES, golden_scene
+from oracle import oracle as O
+from rayfactorcl_gb300 import _lib
+from rayfactorcl_gb300.scene import BV_DTYPE, PRIM_DTYPE, parse_scene_xml
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "rayfactor_gb300.h"
+REFERENCE = Path(os.environ.get("RF_REFERENCE_DIR", "/root/reference"))
+
+
+def _declared():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rf_[A-Za-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_exported_symbols(built_lib):
+    declared = _declared()
+    assert len(declared) >= 20
+    L = ctypes.CDLL(str(built_lib))
+    for name in declared:
+        assert hasattr(L, name), name
+    assert sorted(_lib.EXPORTS) == declared
+
+
+def test_library_loads_without_gpu(built_lib):
+    L = _lib.load()
+    assert L.rf_abi_version() == 1
+    assert L.rf_status_string(6) == b"size overflow"
+
+
+def _compile(src: str, lang: str, tmp_path: Path, extra=()):
+    f = tmp_path / ("t.c" if lang == "c" else "t.cpp")
+    f.write_text(src)
+    exe = tmp_path / "t"
+    cc = "gcc" if lang == "c" else "g++"
+    r = subprocess.run([cc, "-std=c11" if lang == "c" else "-std=c++17", "-Wall", "-Werror",
+                        "-I", str(HEADER.parent), *extra, str(f), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+
+
+@pytest.mark.parametrize("lang", ["c", "cpp"])
+def test_header_compiles_with_reference_layouts(tmp_path, lang):
+    src = """#include "rayfactor_gb300.h"
+#include <stdio.h>
+int main(void) { printf("%d %d %d", (int)sizeof(rf_primitive), (int)sizeof(rf_bounding_volume),
+                        (int)sizeof(rf_config)); return 0; }
+"""
+    out = _compile(src, lang, tmp_path)
+    assert out.split() == ["112", "72", str(ctypes.sizeof(_lib.RfConfig))]
+    assert PRIM_DTYPE.itemsize == 112 and BV_DTYPE.itemsize == 72
+
+
+def test_integration_shim_compiles_against_reference_scene(tmp_path):
+    """The runCL_GPURNG replacement of INTEGRATION.md, compiled with the reference's
+    Scene.h, TinyXML-2 and affine headers (syntax and layout checks only)."""
+    rfc = REFERENCE / "RayFactorCL"
+    if not (rfc / "Scene.h").exists():
+        pytest.skip("reference checkout not present")
+    md = (ROOT / "INTEGRATION.md").read_text()
+    shim = md.split("```cpp", 1)[1].split("```", 1)[0]
+    src = '#include <cstdio>\n#include "Scene.h"\n' + shim
+    f = tmp_path / "shim.cpp"
+    f.write_text(src)
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-w", "-I", str(HEADER.parent), "-I", str(rfc),
+                        "-I", str(rfc / "TinyXML-2"), "-I", str(rfc / "Affine Transformation"), str(f)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def _budgets(sc, n_samples, compat):
+    prims = np.ascontiguousarray(sc.primitives, PRIM_DTYPE)
+    out = np.zeros(sc.n, np.int64)
+    st = _lib.load().rf_ray_budgets(_lib.ptr(prims), sc.n, n_samples, compat, _lib.ptr(out))
+    return st, out
+
+
+@pytest.mark.parametrize("name", SAMPLE_NAMES + GEN_NAMES)
+def test_ray_budgets_follow_reference_rule(built_lib, oracle_lib, name):
+    """main.cpp:172-173 (+178): rays = round_to_128(rayDensity*n/4) * 4; with the
+    compat flag every emitter uses emitter 0's rayDensity."""
+    sc = golden_scene(name)
+    for n_samples in (1000, 12345):
+        st, got = _budgets(sc, n_samples, 0)
+        exp = [O.ref_nthreads(int(r), n_samples) for r in sc.primitives["rayDensity"]]
+        if min(exp) < 0:
+            assert st == 6
+            continue
+        assert st == 0 and list(got) == [4 * e for e in exp]
+        st, got = _budgets(sc, n_samples, _lib.COMPAT_BUDGET)
+        e0 = O.ref_nthreads(int(sc.primitives["rayDensity"][0]), n_samples)
+        assert st == 0 and np.all(got == 4 * e0)
+
+
+def test_ray_budget_overflow_is_an_error(built_lib):
+    sc = golden_scene("input-furnace")  # rayDensity up to 201: 2e7 samples overflow int32 (main.cpp:172)
+    st, _ = _budgets(sc, 20_000_000, 0)
+    assert st == 6
+
+
+def test_output_txt_format(built_lib, tmp_path):
+    """main.cpp:236-249 stores F as float and streams it with precision 8, a comma after
+    every value: compare with the same values through a C++ ostream."""
+    vals = [0.0, 0.171252, 1.0 / 3.0, 1e-9, 0.5, float("nan"), 123456789.0, 2.5e-5, 1.0]
+    F = np.array(vals).reshape(3, 3)
+    path = tmp_path / "output.txt"
+    assert _lib.load().rf_write_output_txt(str(path).encode(), _lib.ptr(F), 3) == 0
+    lits = ", ".join("NAN" if v != v else repr(v) for v in vals)
+    src = """#include <cmath>
+#include <iostream>
+int main() { std::cout.precision(8); const double v[] = {%s};
+  for (int i = 0; i < 3; ++i) { for (int j = 0; j < 3; ++j) std::cout << (float)v[3 * i + j] << ",";
+                                std::cout << std::endl; } return 0; }
+""" % lits
+    expect = _compile(src, "cpp", tmp_path)
+    assert path.read_text() == expect
+    assert expect.splitlines()[0] == "0,0.171252,0.33333334,"
+
+
+def test_create_without_gpu_or_with_bad_config(built_lib):
+    L = _lib.load()
+    cfg = _lib.RfConfig()
+    L.rf_config_default(ctypes.byref(cfg))
+    assert cfg.key1 == 0xDECAFBAD and abs(cfg.eps - 1e-3) < 1e-9 and cfg.compat == 0
+    h = ctypes.c_void_p()
+    bad = _lib.RfConfig.from_buffer_copy(cfg)
+    bad.struct_size = 7
+    assert L.rf_create(ctypes.byref(h), ctypes.byref(bad)) == 1
+    bad = _lib.RfConfig.from_buffer_copy(cfg)
+    bad.precision = 9
+    assert L.rf_create(ctypes.byref(h), ctypes.byref(bad)) == 1
+    bad = _lib.RfConfig.from_buffer_copy(cfg)
+    bad.eps = float("nan")
+    assert L.rf_create(ctypes.byref(h), ctypes.byref(bad)) == 1
+    st = L.rf_create(ctypes.byref(h), ctypes.byref(cfg))
+    if st == 0:
+        L.rf_destroy(h)  # a GPU is present
+    else:
+        assert st == 7  # RF_ERR_NO_DEVICE: no CPU fallback
+
+
+def test_scene_loader_edge_cases():
+    # a comment as the first child of <settings>: the reference loop does not run
+    xml = """<project><settings><!-- c --><globalRayDensity value="5" /></settings>
+             <geometry><primitive type="disc"><scale x="1" y="1" z="1" /></primitive></geometry></project>"""
+    sc = parse_scene_xml(xml)
+    assert sc.global_ray_density == 0.0 and sc.n == 1
+    with pytest.raises(ValueError):
+        parse_scene_xml("<notaproject/>")
+    with pytest.raises(ValueError):
+        parse_scene_xml("""<project><settings><globalRayDensity value="5" /></settings>
+            <geometry><primitive type="annulus"><smallRadius value="1" /></primitive></geometry></project>""")
+    # unknown types are skipped, "true" and integers parse as booleans (tinyxml2.cpp:959-973)
+    sc = parse_scene_xml("""<project><settings><useBoundingVolumes value="1" /></settings>
+        <geometry><bv type="teapot"/></geometry></project>""")
+    assert sc.use_bounding_volumes and sc.bounding_volumes.shape[0] == 0
+
+
+def test_scene_bytes_roundtrip():
+    for name in GEN_NAMES:
+        sc = golden_scene(name)
+        assert type(sc).from_bytes(sc.to_bytes()).to_bytes() == sc.to_bytes()
+
+
+@pytest.mark.parametrize("name", SAMPLE_NAMES)
+def test_loader_matches_reference_on_samples(name):
+    xml = REFERENCE / "sample-geometries" / f"{name}.xml"
+    if not xml.exists():
+        pytest.skip("reference checkout not present")
+    from rayfactorcl_gb300.scene import read_scene
+    assert read_scene(xml).to_bytes() == golden_scene(name).to_bytes()
+
+
+def test_cli_reports_missing_file(built_lib, tmp_path, capsys):
+    from rayfactorcl_gb300.__main__ import main
+    assert main([str(tmp_path / "missing.xml")]) == 1
