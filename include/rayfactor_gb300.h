@@ -194,10 +194,19 @@ rf_status rf_converge_batch(rf_ctx *ctx, const rf_scene_desc *scenes, int32_t n_
 rf_status rf_check_F(rf_ctx *ctx, const double *F, const double *areas, int32_t n,
                      double *max_sum_err, double *max_recip_err);
 
-/* Pick block size, rays per thread and tallying for the current scene by
- * timing short runs; the choice is cached per scene shape in memory and, when
- * cache_path is not NULL, in that file.  Applies the choice to the context. */
+/* Pick the launch shape of the single-scene kernels for the current scene by
+ * timing short runs (about 2^22 rays) of every combination of threads per block
+ * (128, 256), rays per thread (4, 8), surface staging (shared-memory tiles or
+ * reads through L1) and tallying (shared-memory row histogram or global
+ * atomics); the choice is cached per scene shape in memory and, when cache_path
+ * is not NULL, appended to that file and read back by later processes.  Applies
+ * the choice to the context.  A no-op for RF_PREC_MIXED (one launch shape).
+ * Results of a trace do not depend on the launch shape. */
 rf_status rf_autotune(rf_ctx *ctx, int32_t use_bv, const char *cache_path);
+
+/* The launch shape the context uses now (after rf_autotune, or the defaults). */
+rf_status rf_get_launch_config(rf_ctx *ctx, int32_t *block, int32_t *rays_per_thread,
+                               int32_t *smem_hist, int32_t *smem_table);
 
 /* Counters of the last mixed-precision run: tests re-evaluated in FP64. */
 rf_status rf_last_refine_count(rf_ctx *ctx, uint64_t *refined_tests);

@@ -34,7 +34,7 @@ EXPORTS = ("rf_config_default", "rf_create", "rf_destroy", "rf_last_error", "rf_
            "rf_last_trace_stats", "rf_stream", "rf_trace_rays", "rf_run_gpurng", "rf_ray_budgets",
            "rf_write_output_txt", "rf_trace_batch", "rf_converge_batch", "rf_check_F",
            "rf_autotune", "rf_last_refine_count", "rf_last_work_counts", "rf_measure_fp32_peak",
-           "rf_trace_mixed_noalloc")
+           "rf_trace_mixed_noalloc", "rf_get_launch_config")
 
 
 class RfConfig(ctypes.Structure):
@@ -90,6 +90,7 @@ def load() -> ctypes.CDLL:
         "rf_check_F": (ctypes.c_int, [P, P, P, I32, ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(ctypes.c_double)]),
         "rf_autotune": (ctypes.c_int, [P, I32, ctypes.c_char_p]),
+        "rf_get_launch_config": (ctypes.c_int, [P, P, P, P, P]),
         "rf_last_refine_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
         "rf_last_work_counts": (ctypes.c_int, [P, P]),
         "rf_measure_fp32_peak": (ctypes.c_int, [I32, ctypes.POINTER(ctypes.c_double)]),

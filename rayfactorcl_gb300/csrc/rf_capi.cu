@@ -9,7 +9,11 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
 #include <new>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -94,8 +98,8 @@ struct rf_ctx {
     int last_launches = 0;
     bool timed = false;
 
-    // launch choices (0 = default); set by rf_config or rf_autotune
-    int block = 0, gpt = 0, hist = -1;
+    // launch choices (0 / -1 = default); set by rf_config or rf_autotune
+    int block = 0, gpt = 0, hist = -1, stage = -1;
 
     // batched mixed-precision path: scenes concatenated, re-centred in FP64
     DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters;
@@ -217,6 +221,7 @@ int64_t plan_segments(std::vector<Segment> &seg, int emitter, int scene, int64_t
 struct Plan {
     LaunchCfg lc;
     bool hist = false;
+    bool stage = true;
 };
 
 // Launch shape for the single-scene kernels.
@@ -231,7 +236,8 @@ Plan make_plan(rf_ctx *c, bool bv, bool rec)
     if (bv || rec || c->cfg.precision == RF_PREC_FP64) gpt = 1;
     pl.lc.gpt = gpt;
     pl.hist = !rec && (c->hist >= 0 ? c->hist == 1 : true) && c->n <= kHistMax;
-    const int tab = bv ? 0 : std::min(c->n, kTile);
+    pl.stage = !bv && (c->stage >= 0 ? c->stage == 1 : true);
+    const int tab = pl.stage ? std::min(c->n, kTile) : 0;
     pl.lc.smem = (size_t)tab * sizeof(HitRec) + (pl.hist ? (size_t)c->n * 4 : 0);
     return pl;
 }
@@ -271,6 +277,7 @@ rf_status run_trace(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_ch
     p.scene_id = c->cfg.scene_id;
     p.eps = c->cfg.eps;
     p.use_smem_hist = pl.hist ? 1 : 0;
+    p.stage_table = pl.stage ? 1 : 0;
 
     const int arith = arith_of(c);
     int bps = blocks_per_sm(arith, pl.lc);
@@ -1043,9 +1050,139 @@ rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_sc
     return RF_OK;
 }
 
-rf_status rf_autotune(rf_ctx *c, int32_t, const char *)
+// Autotuner of the single-scene kernels: times every launch shape on a short
+// trace of the current scene and keeps the fastest.  Knobs: threads per block
+// (128 / 256), Philox draws per thread (1 / 2, i.e. 4 or 8 rays in registers),
+// surface staging (shared-memory tiles / reads through L1) and tallying (row
+// histogram in shared memory / warp-aggregated global atomics).  Results are
+// cached per scene shape (precision, kernel, surface count and type mix, SM
+// count) in memory and, optionally, in a text file of "key|block gpt hist stage"
+// lines.  The mixed-precision kernel has one launch shape (a persistent grid of
+// 1024-thread blocks) and needs no tuning.
+namespace {
+struct TuneChoice {
+    int block, gpt, hist, stage;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneChoice> g_tune_cache;
+
+std::string tune_key(const rf_ctx *c, int use_bv)
 {
-    return fail(c, RF_ERR_UNSUPPORTED, "autotuner not built in this library");
+    int types[6] = {0, 0, 0, 0, 0, 0};
+    for (const rf_primitive &p : c->prims) ++types[p.type];
+    std::ostringstream k;
+    k << "v1 prec=" << c->cfg.precision << " bv=" << use_bv << " n=" << c->n << " nbv=" << c->nbv << " t=";
+    for (int i = 0; i < 6; ++i) k << types[i] << (i < 5 ? "," : "");
+    k << " sm=" << c->sms;
+    return k.str();
+}
+
+bool tune_lookup_file(const char *path, const std::string &key, TuneChoice &out)
+{
+    std::ifstream f(path);
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {
+        const size_t bar = line.find('|');
+        if (bar == std::string::npos || line.compare(0, bar, key) != 0 || bar != key.size()) continue;
+        std::istringstream v(line.substr(bar + 1));
+        TuneChoice t{};
+        if (v >> t.block >> t.gpt >> t.hist >> t.stage) {
+            out = t;
+            found = true;  // the last entry wins
+        }
+    }
+    return found;
+}
+
+void tune_apply(rf_ctx *c, const TuneChoice &t)
+{
+    c->block = t.block;
+    c->gpt = t.gpt;
+    c->hist = t.hist;
+    c->stage = t.stage;
+}
+}  // namespace
+
+rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
+{
+    rf_status s = require_scene(c);
+    if (s != RF_OK) return s;
+    if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
+    if (c->cfg.precision == RF_PREC_MIXED) return RF_OK;  // one launch shape
+    const std::string key = tune_key(c, use_bv ? 1 : 0);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            tune_apply(c, it->second);
+            return RF_OK;
+        }
+    }
+    TuneChoice best{};
+    if (cache_path && tune_lookup_file(cache_path, key, best)) {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = best;
+        tune_apply(c, best);
+        return RF_OK;
+    }
+    // a short trace: about 2^22 rays over the emitters
+    const int64_t per = std::max<int64_t>(1024, ((int64_t)1 << 22) / c->n) / 4 * 4;
+    std::vector<int64_t> rays(c->n, per);
+    const bool bv = use_bv != 0;
+    const bool wide = !bv && c->cfg.precision != RF_PREC_FP64;
+    double best_ms = 1e300;
+    const TuneChoice saved{c->block, c->gpt, c->hist, c->stage};
+    for (int block : {128, 256})
+        for (int gpt : {1, 2}) {
+            if (gpt == 2 && !wide) continue;
+            for (int hist : {1, 0}) {
+                if (hist && c->n > kHistMax) continue;
+                for (int stage : {1, 0}) {
+                    if (bv && stage == 0) continue;  // the bounding-surface kernel reads through L1 anyway
+                    tune_apply(c, TuneChoice{block, gpt, hist, stage});
+                    double ms_min = 1e300;
+                    for (int rep = 0; rep < 4; ++rep) {
+                        if ((s = rf_trace_async(c, rays.data(), use_bv)) != RF_OK) {
+                            tune_apply(c, saved);
+                            return s;
+                        }
+                        double ms = 0.0;
+                        if ((s = rf_last_trace_stats(c, &ms, nullptr)) != RF_OK) {
+                            tune_apply(c, saved);
+                            return s;
+                        }
+                        if (rep > 0) ms_min = std::min(ms_min, ms);  // the first run warms up
+                    }
+                    if (ms_min < best_ms) {
+                        best_ms = ms_min;
+                        best = TuneChoice{block, gpt, hist, stage};
+                    }
+                }
+            }
+        }
+    c->have_results = false;
+    tune_apply(c, best);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = best;
+    }
+    if (cache_path) {
+        std::ofstream f(cache_path, std::ios::app);
+        if (f) f << key << "|" << best.block << " " << best.gpt << " " << best.hist << " " << best.stage << "\n";
+    }
+    return RF_OK;
+}
+
+rf_status rf_get_launch_config(rf_ctx *c, int32_t *block, int32_t *rays_per_thread, int32_t *smem_hist,
+                               int32_t *smem_table)
+{
+    if (!c) return RF_ERR_INVALID_ARG;
+    if (block) *block = c->block > 0 ? c->block : (c->cfg.block_size > 0 ? c->cfg.block_size : kBlock);
+    if (rays_per_thread) *rays_per_thread = 4 * (c->gpt > 0 ? c->gpt : (c->cfg.rays_per_thread == 8 ? 2 : 1));
+    if (smem_hist) *smem_hist = c->hist >= 0 ? c->hist : 1;
+    if (smem_table) *smem_table = c->stage >= 0 ? c->stage : 1;
+    return RF_OK;
 }
 
 rf_status rf_last_work_counts(rf_ctx *c, uint64_t *counts)

@@ -57,6 +57,7 @@ struct TraceParams {
     uint32_t scene_id;
     float eps;
     int32_t use_smem_hist;          // 1: shared-memory row histogram, 0: global atomics
+    int32_t stage_table;            // plain kernel: 1 stage surfaces in smem tiles, 0 read through L1
     const float4 *bsph;             // batched kernel: world bounding sphere per surface
     const int64_t *d_total;         // batched kernel: device-resident chunk count (or null)
     const int32_t *d_nseg;          // batched kernel: device-resident segment count (or null)

@@ -90,8 +90,9 @@ __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
 
     const int n = p.n;
     const int tid = threadIdx.x;
-    const bool tiled = !BV && n > kTile;
-    const int tab_cap = BV ? 0 : (tiled ? kTile : n);
+    const bool stage = !BV && p.stage_table;  // surfaces in smem tiles, else through L1
+    const bool tiled = stage && n > kTile;
+    const int tab_cap = stage ? (tiled ? kTile : n) : 0;
     HitRec *s_tab = reinterpret_cast<HitRec *>(smem);
     int *s_hist = reinterpret_cast<int *>(smem + (size_t)tab_cap * sizeof(HitRec));
     const bool hist = !REC && p.use_smem_hist;
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
 
     if (hist)
         for (int i = tid; i < n; i += blockDim.x) s_hist[i] = 0;
-    if (!BV && !tiled) {
+    if (stage && !tiled) {
         const float4 *src = reinterpret_cast<const float4 *>(p.tab);
         float4 *dst = reinterpret_cast<float4 *>(s_tab);
         for (int i = tid; i < 4 * n; i += blockDim.x) dst[i] = __ldg(src + i);
@@ -171,8 +172,9 @@ __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
             T tb[R];
 #pragma unroll
             for (int k = 0; k < R; ++k) { tb[k] = M::inf(); bi[k] = -1; }
-            for (int t0 = 0; t0 < n; t0 += kTile) {
-                const int cnt = min(kTile, n - t0);
+            const int step = stage ? kTile : n;
+            for (int t0 = 0; t0 < n; t0 += step) {
+                const int cnt = min(step, n - t0);
                 if (tiled) {
                     __syncthreads();
                     const float4 *src = reinterpret_cast<const float4 *>(p.tab + t0);
@@ -181,7 +183,7 @@ __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
                     __syncthreads();
                 }
                 for (int jj = 0; jj < cnt; ++jj) {
-                    const HitRec h = s_tab[jj];
+                    const HitRec h = stage ? s_tab[jj] : load_rec(p.tab, t0 + jj);
                     const int j = t0 + jj;
                     switch (__float_as_int(h.aux.x)) {  // warp-uniform
 #define RF_TEST_ALL(call)                                               \

@@ -128,6 +128,18 @@ class Tracer:
                                           ptr(hits), ptr(F)))
         return rays, hits.astype(np.int64), F
 
+    def autotune(self, use_bv: bool = False, cache_path: str | None = None):
+        """Time the launch shapes of the current scene and keep the fastest."""
+        self._check(self._L.rf_autotune(self._h, 1 if use_bv else 0,
+                                        None if cache_path is None else str(cache_path).encode()))
+        return self.launch_config()
+
+    def launch_config(self) -> dict:
+        v = [ctypes.c_int32() for _ in range(4)]
+        self._check(self._L.rf_get_launch_config(self._h, *[ctypes.byref(x) for x in v]))
+        return {"block": v[0].value, "rays_per_thread": v[1].value, "smem_hist": v[2].value,
+                "smem_table": v[3].value}
+
     def refined_count(self) -> int:
         """Quadric tests re-evaluated in FP64 by the last mixed-precision run."""
         v = ctypes.c_uint64()

@@ -191,3 +191,26 @@ def test_single_primitive_and_empty_budgets(built_lib, oracle_lib):
         hits, F = t.trace([4001])
     exp = O.tally(sc, O.params(compat=0), np.array([4001]))
     assert np.array_equal(hits, exp)
+
+
+@pytest.mark.parametrize("name,prec", [("gen_mixed64", PREC_EXACT), ("gen_furnace", PREC_EXACT),
+                                       ("gen_sweep0", PREC_FAST)])
+def test_autotune_keeps_results(built_lib, tmp_path, name, prec):
+    """Every launch shape the autotuner may pick gives the same tallies; the choice is
+    cached in memory and in the file."""
+    sc = golden_scene(name)
+    use_bv = bool(sc.use_bounding_volumes)
+    rays = np.full(sc.n, 2000 if sc.n < 100 else 300, np.int64)
+    with _tracer(sc, precision=prec) as t:
+        ref, _ = t.trace(rays, use_bv=use_bv)
+    cache = tmp_path / "tune.txt"
+    with _tracer(sc, precision=prec) as t:
+        cfg = t.autotune(use_bv=use_bv, cache_path=cache)
+        got, _ = t.trace(rays, use_bv=use_bv)
+    assert np.array_equal(got, ref)
+    assert cfg["block"] in (128, 256) and cfg["rays_per_thread"] in (4, 8)
+    lines = cache.read_text().splitlines()
+    assert len(lines) == 1 and "|" in lines[0]
+    with _tracer(sc, precision=prec) as t2:
+        assert t2.autotune(use_bv=use_bv, cache_path=cache) == cfg
+    assert len(cache.read_text().splitlines()) == 1  # served from the cache
