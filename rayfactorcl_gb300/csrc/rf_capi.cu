@@ -1126,8 +1126,9 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
         tune_apply(c, best);
         return RF_OK;
     }
-    // a short trace: about 2^22 rays over the emitters
-    const int64_t per = std::max<int64_t>(1024, ((int64_t)1 << 22) / c->n) / 4 * 4;
+    // trials long enough for the steady state of a persistent wave: about 2^25
+    // rays over the emitters (a few ms each)
+    const int64_t per = std::max<int64_t>(4096, ((int64_t)1 << 25) / c->n) / 4 * 4;
     std::vector<int64_t> rays(c->n, per);
     const bool bv = use_bv != 0;
     const bool wide = !bv && c->cfg.precision != RF_PREC_FP64;
@@ -1142,7 +1143,7 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
                     if (bv && stage == 0) continue;  // the bounding-surface kernel reads through L1 anyway
                     tune_apply(c, TuneChoice{block, gpt, hist, stage});
                     double ms_min = 1e300;
-                    for (int rep = 0; rep < 4; ++rep) {
+                    for (int rep = 0; rep < 3; ++rep) {
                         if ((s = rf_trace_async(c, rays.data(), use_bv)) != RF_OK) {
                             tune_apply(c, saved);
                             return s;
