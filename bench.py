@@ -226,6 +226,8 @@ def run_ours(args):
     # -- headline kernel: scene resident, per-step device time ------------
     t, stream = tracer(headline)
     if headline != PREC_MIXED:
+        t.trace_async(rays)
+        t.read_results(None, None)
         t.autotune()
     barrier()
     torch.cuda.synchronize()
@@ -277,6 +279,8 @@ def run_ours(args):
     plain = None
     if headline != PREC_EXACT and not args.no_plain:
         tp, sp = tracer(PREC_EXACT)
+        tp.trace_async(rays)  # the workload's budgets, which the autotuner then tunes for
+        tp.read_results(None, None)
         plain_cfg = tp.autotune()  # the plain kernel at its best launch shape
         p_step, p_kern = time_trace(tp, rays, args.steps, args.warmup, l2_flush, sp)
         tp.close()

@@ -195,7 +195,8 @@ rf_status rf_check_F(rf_ctx *ctx, const double *F, const double *areas, int32_t 
                      double *max_sum_err, double *max_recip_err);
 
 /* Pick the launch shape of the single-scene kernels for the current scene by
- * timing runs of about 2^25 rays of every combination of threads per block
+ * timing runs of about 2^25 rays (spread over the emitters like the budgets of
+ * the context's last trace, else evenly) of every combination of threads per block
  * (128, 256), rays per thread (4, 8), surface staging (shared-memory tiles or
  * reads through L1) and tallying (shared-memory row histogram or global
  * atomics); the choice is cached per scene shape in memory and, when cache_path

@@ -1127,9 +1127,16 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
         return RF_OK;
     }
     // trials long enough for the steady state of a persistent wave: about 2^25
-    // rays over the emitters (a few ms each)
-    const int64_t per = std::max<int64_t>(4096, ((int64_t)1 << 25) / c->n) / 4 * 4;
-    std::vector<int64_t> rays(c->n, per);
+    // rays (a few ms each), spread like the last trace's budgets when there was
+    // one (the workload being tuned for), else evenly
+    const double target = (double)((int64_t)1 << 25);
+    std::vector<int64_t> rays(c->n, std::max<int64_t>(4096, ((int64_t)1 << 25) / c->n) / 4 * 4);
+    if ((int)c->last_rays.size() == c->n) {
+        double tot = 0.0;
+        for (int64_t r : c->last_rays) tot += (double)r;
+        if (tot > 0.0)
+            for (int e = 0; e < c->n; ++e) rays[e] = (int64_t)(target * (double)c->last_rays[e] / tot) / 4 * 4;
+    }
     const bool bv = use_bv != 0;
     const bool wide = !bv && c->cfg.precision != RF_PREC_FP64;
     double best_ms = 1e300;
