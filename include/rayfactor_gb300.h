@@ -97,7 +97,9 @@ typedef struct rf_config {
     int32_t block_size;   /* 0: autotuned / built-in default                                */
     int32_t rays_per_thread; /* 0: default; 4 or 8 (one or two Philox draws)                */
     uint32_t scene_id;    /* folded into the stream counter outside RF_COMPAT_STREAMS       */
-    uint32_t reserved[7];
+    int32_t tally_mode;   /* 0: autotuned / default; 1: shared-memory row histogram; 2: global atomics */
+    int32_t table_mode;   /* 0: autotuned / default; 1: surfaces staged in shared memory; 2: read through L1 */
+    uint32_t reserved[5];
 } rf_config;
 
 typedef struct rf_ctx rf_ctx;

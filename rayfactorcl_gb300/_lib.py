@@ -42,7 +42,8 @@ class RfConfig(ctypes.Structure):
                 ("precision", ctypes.c_uint32), ("key1", ctypes.c_uint32), ("eps", ctypes.c_float),
                 ("device", ctypes.c_int32), ("block_size", ctypes.c_int32),
                 ("rays_per_thread", ctypes.c_int32), ("scene_id", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 7)]
+                ("tally_mode", ctypes.c_int32), ("table_mode", ctypes.c_int32),
+                ("reserved", ctypes.c_uint32 * 5)]
 
 
 class RfSceneDesc(ctypes.Structure):

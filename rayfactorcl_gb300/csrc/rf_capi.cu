@@ -557,6 +557,7 @@ rf_status rf_create(rf_ctx **out, const rf_config *cfg)
     if (c.rays_per_thread != 0 && c.rays_per_thread != 4 && c.rays_per_thread != 8)
         return RF_ERR_INVALID_ARG;
     if (c.block_size < 0 || c.block_size > kBlock || (c.block_size % 32) != 0) return RF_ERR_INVALID_ARG;
+    if (c.tally_mode < 0 || c.tally_mode > 2 || c.table_mode < 0 || c.table_mode > 2) return RF_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
         cudaGetLastError();
@@ -567,6 +568,8 @@ rf_status rf_create(rf_ctx **out, const rf_config *cfg)
     if (!ctx) return RF_ERR_OOM;
     ctx->cfg = c;
     ctx->device = c.device;
+    if (c.tally_mode) ctx->hist = c.tally_mode == 1 ? 1 : 0;
+    if (c.table_mode) ctx->stage = c.table_mode == 1 ? 1 : 0;
     if (cudaSetDevice(c.device) != cudaSuccess ||
         cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||

@@ -28,7 +28,7 @@ class Tracer:
 
     def __init__(self, precision: int = PREC_EXACT, compat: int = 0, key1: int = REF_KEY1,
                  eps: float = 1e-3, device: int = 0, block_size: int = 0, rays_per_thread: int = 0,
-                 scene_id: int = 0):
+                 scene_id: int = 0, tally_mode: int = 0, table_mode: int = 0):
         L = _lib.load()
         cfg = _lib.RfConfig()
         L.rf_config_default(ctypes.byref(cfg))
@@ -40,6 +40,8 @@ class Tracer:
         cfg.block_size = block_size
         cfg.rays_per_thread = rays_per_thread
         cfg.scene_id = scene_id & 0xFFFFFFFF
+        cfg.tally_mode = tally_mode
+        cfg.table_mode = table_mode
         h = ctypes.c_void_p()
         check(L.rf_create(ctypes.byref(h), ctypes.byref(cfg)))
         self._h = h
