@@ -236,7 +236,8 @@ Plan make_plan(rf_ctx *c, bool bv, bool rec)
     if (bv || rec || c->cfg.precision == RF_PREC_FP64) gpt = 1;
     pl.lc.gpt = gpt;
     pl.hist = !rec && (c->hist >= 0 ? c->hist == 1 : true) && c->n <= kHistMax;
-    pl.stage = !bv && (c->stage >= 0 ? c->stage == 1 : true);
+    pl.stage = !bv && (rec || (c->stage >= 0 ? c->stage == 1 : true));
+    pl.lc.stage = pl.stage;
     const int tab = pl.stage ? std::min(c->n, kTile) : 0;
     pl.lc.smem = (size_t)tab * sizeof(HitRec) + (pl.hist ? (size_t)c->n * 4 : 0);
     return pl;
@@ -277,7 +278,6 @@ rf_status run_trace(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_ch
     p.scene_id = c->cfg.scene_id;
     p.eps = c->cfg.eps;
     p.use_smem_hist = pl.hist ? 1 : 0;
-    p.stage_table = pl.stage ? 1 : 0;
 
     const int arith = arith_of(c);
     int bps = blocks_per_sm(arith, pl.lc);

@@ -57,7 +57,6 @@ struct TraceParams {
     uint32_t scene_id;
     float eps;
     int32_t use_smem_hist;          // 1: shared-memory row histogram, 0: global atomics
-    int32_t stage_table;            // plain kernel: 1 stage surfaces in smem tiles, 0 read through L1
     const float4 *bsph;             // batched kernel: world bounding sphere per surface
     const int64_t *d_total;         // batched kernel: device-resident chunk count (or null)
     const int32_t *d_nseg;          // batched kernel: device-resident segment count (or null)
@@ -80,6 +79,7 @@ struct LaunchCfg {
     size_t smem = 0;
     bool bv = false;    // runBVGPU semantics
     bool rec = false;   // write per-ray hit indices instead of tallying
+    bool stage = true;  // surfaces staged in shared memory (else read through L1)
 };
 
 // Implemented once per arithmetic policy (rf_kern_exact.cu, rf_kern_fast.cu).

@@ -80,7 +80,7 @@ __device__ __forceinline__ int trace_bv(const TraceParams &p, const Ray<typename
     return obj;
 }
 
-template <class M, int GPT, bool BV, bool REC>
+template <class M, int GPT, bool BV, bool REC, bool STAGE>
 __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
 {
     using T = typename M::T;
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
 
     const int n = p.n;
     const int tid = threadIdx.x;
-    const bool stage = !BV && p.stage_table;  // surfaces in smem tiles, else through L1
+    constexpr bool stage = !BV && STAGE;  // surfaces in smem tiles, else through L1
     const bool tiled = stage && n > kTile;
     const int tab_cap = stage ? (tiled ? kTile : n) : 0;
     HitRec *s_tab = reinterpret_cast<HitRec *>(smem);
@@ -223,10 +223,10 @@ __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
     if (hist && sg.emitter >= 0) flush(sg.emitter);
 }
 
-template <class M, int GPT, bool BV, bool REC>
+template <class M, int GPT, bool BV, bool REC, bool STAGE>
 static cudaError_t launch_one(const LaunchCfg &cfg, const TraceParams &p, cudaStream_t st)
 {
-    auto k = trace_kernel<M, GPT, BV, REC>;
+    auto k = trace_kernel<M, GPT, BV, REC, STAGE>;
     if (cfg.smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
         if (e != cudaSuccess) return e;
@@ -235,11 +235,11 @@ static cudaError_t launch_one(const LaunchCfg &cfg, const TraceParams &p, cudaSt
     return cudaGetLastError();
 }
 
-template <class M, int GPT, bool BV, bool REC>
+template <class M, int GPT, bool BV, bool REC, bool STAGE>
 static int occupancy_one(const LaunchCfg &cfg)
 {
     int nb = 0;
-    auto k = trace_kernel<M, GPT, BV, REC>;
+    auto k = trace_kernel<M, GPT, BV, REC, STAGE>;
     if (cfg.smem > 48 * 1024)
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, cfg.block, cfg.smem) != cudaSuccess)
@@ -250,12 +250,16 @@ static int occupancy_one(const LaunchCfg &cfg)
 #define RF_DISPATCH(FN, ...)                                                        \
     do {                                                                            \
         if (cfg.rec) {                                                              \
-            if (cfg.bv) return FN<M, 1, true, true>(__VA_ARGS__);                   \
-            return FN<M, 1, false, true>(__VA_ARGS__);                              \
+            if (cfg.bv) return FN<M, 1, true, true, false>(__VA_ARGS__);            \
+            return FN<M, 1, false, true, true>(__VA_ARGS__);                        \
         }                                                                           \
-        if (cfg.bv) return FN<M, 1, true, false>(__VA_ARGS__);                      \
-        if (cfg.gpt == 2) return FN<M, 2, false, false>(__VA_ARGS__);               \
-        return FN<M, 1, false, false>(__VA_ARGS__);                                 \
+        if (cfg.bv) return FN<M, 1, true, false, false>(__VA_ARGS__);               \
+        if (cfg.gpt == 2) {                                                         \
+            if (cfg.stage) return FN<M, 2, false, false, true>(__VA_ARGS__);        \
+            return FN<M, 2, false, false, false>(__VA_ARGS__);                      \
+        }                                                                           \
+        if (cfg.stage) return FN<M, 1, false, false, true>(__VA_ARGS__);            \
+        return FN<M, 1, false, false, false>(__VA_ARGS__);                          \
     } while (0)
 
 template <class M>
