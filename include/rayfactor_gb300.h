@@ -127,6 +127,20 @@ rf_status rf_set_scene(rf_ctx *ctx, const rf_primitive *prims, int32_t n_prims,
 rf_status rf_trace(rf_ctx *ctx, const int64_t *rays_per_emitter, int32_t use_bv,
                    uint64_t *hits_out, double *F_out);
 
+/* Trace rays [first_ray[e], first_ray[e] + count[e]) of every emitter e and add
+ * the tallies to the context's running tallies (accumulate = 1, after a trace or
+ * rf_set_tallies) or start new ones (accumulate = 0).  A ray's stream depends
+ * only on (emitter, ray index), so a run split into ranges -- resumed from a
+ * checkpoint, or divided between processes whose tallies are summed -- gives
+ * exactly the tallies of one run.  Asynchronous like rf_trace_async;
+ * rf_read_results normalises by all rays traced so far. */
+rf_status rf_trace_range(rf_ctx *ctx, const int64_t *first_ray, const int64_t *count,
+                         int32_t use_bv, int32_t accumulate);
+
+/* Restore running tallies and ray counts (a checkpoint: n x n tallies and the
+ * rays traced per emitter), to continue with rf_trace_range(accumulate = 1). */
+rf_status rf_set_tallies(rf_ctx *ctx, const uint64_t *hits, const int64_t *rays_per_emitter);
+
 /* The same, split for callers that time or overlap the GPU work:
  * rf_trace_async enqueues on the context's stream and returns; rf_read_results
  * waits and copies the tallies (and F) of the last trace. */
@@ -157,6 +171,18 @@ rf_status rf_run_gpurng(rf_ctx *ctx, int32_t n_samples, int32_t use_bv, int64_t 
 /* The budget rule alone (host arithmetic, no GPU). */
 rf_status rf_ray_budgets(const rf_primitive *prims, int32_t n_prims, int32_t n_samples,
                          uint32_t compat, int64_t *rays_out);
+
+/* Surface area of every primitive under its affine transform, in FP64 (closed
+ * form for the planar types, quadrature of the parametric surface for
+ * cylinders, frusta and spheres; exact for non-uniform scaling, unlike the
+ * rayDensity proxies of Scene.cpp:361-387). */
+rf_status rf_surface_areas(const rf_primitive *prims, int32_t n_prims, double *areas_out);
+
+/* Budget planner: total_rays spread over the emitters in proportion to their
+ * areas, in multiples of four (one Philox draw), at least four per non-empty
+ * surface.  No int32 limits (compare main.cpp:172). */
+rf_status rf_budgets_by_area(const rf_primitive *prims, int32_t n_prims, int64_t total_rays,
+                             int64_t *rays_out);
 
 /* Write F like main.cpp:236-249: one row per emitter, 8 significant digits,
  * every value followed by a comma. */

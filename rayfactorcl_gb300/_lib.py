@@ -34,7 +34,8 @@ EXPORTS = ("rf_config_default", "rf_create", "rf_destroy", "rf_last_error", "rf_
            "rf_last_trace_stats", "rf_stream", "rf_trace_rays", "rf_run_gpurng", "rf_ray_budgets",
            "rf_write_output_txt", "rf_trace_batch", "rf_converge_batch", "rf_check_F",
            "rf_autotune", "rf_last_refine_count", "rf_last_work_counts", "rf_measure_fp32_peak",
-           "rf_trace_mixed_noalloc", "rf_get_launch_config")
+           "rf_trace_mixed_noalloc", "rf_get_launch_config", "rf_trace_range", "rf_set_tallies",
+           "rf_surface_areas", "rf_budgets_by_area")
 
 
 class RfConfig(ctypes.Structure):
@@ -92,6 +93,10 @@ def load() -> ctypes.CDLL:
                                       ctypes.POINTER(ctypes.c_double)]),
         "rf_autotune": (ctypes.c_int, [P, I32, ctypes.c_char_p]),
         "rf_get_launch_config": (ctypes.c_int, [P, P, P, P, P]),
+        "rf_trace_range": (ctypes.c_int, [P, P, P, I32, I32]),
+        "rf_set_tallies": (ctypes.c_int, [P, P, P]),
+        "rf_surface_areas": (ctypes.c_int, [P, I32, P]),
+        "rf_budgets_by_area": (ctypes.c_int, [P, I32, I64, P]),
         "rf_last_refine_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
         "rf_last_work_counts": (ctypes.c_int, [P, P]),
         "rf_measure_fp32_peak": (ctypes.c_int, [I32, ctypes.POINTER(ctypes.c_double)]),

@@ -691,6 +691,62 @@ rf_status rf_trace_async(rf_ctx *c, const int64_t *rays, int32_t use_bv)
     return RF_OK;
 }
 
+rf_status rf_trace_range(rf_ctx *c, const int64_t *first_ray, const int64_t *count, int32_t use_bv,
+                         int32_t accumulate)
+{
+    rf_status s = require_scene(c);
+    if (s != RF_OK) return s;
+    if (!first_ray || !count) return fail(c, RF_ERR_INVALID_ARG, "first_ray / count is NULL");
+    if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
+    if (use_bv && c->cfg.precision == RF_PREC_MIXED)
+        return fail(c, RF_ERR_UNSUPPORTED, "bounding-surface semantics need EXACT, FAST or FP64");
+    if (accumulate && (int)c->last_rays.size() != c->n)
+        return fail(c, RF_ERR_STATE, "nothing to accumulate into: trace or rf_set_tallies first");
+    std::vector<int64_t> ends(c->n);
+    for (int e = 0; e < c->n; ++e) {
+        if (first_ray[e] < 0 || count[e] < 0) return fail(c, RF_ERR_INVALID_ARG, "negative ray range (emitter %d)", e);
+        ends[e] = first_ray[e] + count[e];
+    }
+    if ((s = check_budgets(c, ends.data(), c->n)) != RF_OK) return s;
+    RF_CUDA(c, cudaSetDevice(c->device));
+    std::vector<Segment> seg;
+    int64_t chunks = 0;
+    const bool mixed = c->cfg.precision == RF_PREC_MIXED;
+    Plan pl = make_plan(c, use_bv != 0, false);
+    const int64_t chunk_gids = mixed ? kBatchChunkDraws : (int64_t)pl.lc.block * pl.lc.gpt;
+    for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, first_ray[e], count[e], chunk_gids, chunks);
+    if (!accumulate) c->last_rays.assign(c->n, 0);
+    for (int e = 0; e < c->n; ++e) c->last_rays[e] += count[e];
+    c->have_results = false;
+    if (mixed) {
+        if (!c->b_single) return fail(c, RF_ERR_STATE, "scene not prepared for the mixed kernel");
+        s = run_batched(c, seg, chunks, false, nullptr, 0, !accumulate);
+    } else {
+        s = run_trace(c, seg, chunks, pl, nullptr, 0, !accumulate);
+    }
+    if (s != RF_OK) return s;
+    c->have_results = true;
+    return RF_OK;
+}
+
+rf_status rf_set_tallies(rf_ctx *c, const uint64_t *hits, const int64_t *rays)
+{
+    rf_status s = require_scene(c);
+    if (s != RF_OK) return s;
+    if (!hits || !rays) return fail(c, RF_ERR_INVALID_ARG, "hits / rays is NULL");
+    for (int e = 0; e < c->n; ++e)
+        if (rays[e] < 0) return fail(c, RF_ERR_INVALID_ARG, "negative ray count (emitter %d)", e);
+    RF_CUDA(c, cudaSetDevice(c->device));
+    const size_t nn = (size_t)c->n * c->n;
+    DevBuf &dst = c->cfg.precision == RF_PREC_MIXED ? c->b_hits : c->d_hits;
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(dst.p, hits, nn * 8, cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->last_rays.assign(rays, rays + c->n);
+    c->have_results = true;
+    return RF_OK;
+}
+
 rf_status rf_read_results(rf_ctx *c, uint64_t *hits_out, double *F_out)
 {
     rf_status s = require_scene(c);
@@ -815,6 +871,102 @@ rf_status rf_run_gpurng(rf_ctx *c, int32_t n_samples, int32_t use_bv, int64_t *r
         return fail(c, s, "ray budget rayDensity*n_samples overflows int32 (main.cpp:172)");
     if (rays_out) std::copy(rays.begin(), rays.end(), rays_out);
     return rf_trace(c, rays.data(), use_bv, hits_out, F_out);
+}
+
+namespace {
+
+// |a x b| of two 3-vectors
+double cross_norm(const double a[3], const double b[3])
+{
+    const double x = a[1] * b[2] - a[2] * b[1], y = a[2] * b[0] - a[0] * b[2], z = a[0] * b[1] - a[1] * b[0];
+    return std::sqrt(x * x + y * y + z * z);
+}
+
+// M v for the linear part of a row-major 3x4 transform
+void lin(const float *m, const double v[3], double out[3])
+{
+    for (int k = 0; k < 3; ++k) out[k] = m[4 * k] * v[0] + m[4 * k + 1] * v[1] + m[4 * k + 2] * v[2];
+}
+
+// Area of a surface of revolution patch p(theta, z) = M (rho(z) cos, rho(z) sin, z)
+// (rho = 1 + (top-1) z, or the unit sphere when sphere is set): the periodic
+// direction by the trapezoid rule, the other by composite Gauss-Legendre.
+double revolution_area(const float *m, double top, bool sphere)
+{
+    static const double gx[4] = {-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526};
+    static const double gw[4] = {0.3478548451374538, 0.6521451548625461, 0.6521451548625461, 0.3478548451374538};
+    const int NT = 256, NZ = 64;  // theta samples; z panels of 4 points
+    double area = 0.0;
+    for (int iz = 0; iz < NZ; ++iz)
+        for (int q = 0; q < 4; ++q) {
+            // sphere: parameter u in [-pi/2, pi/2] (latitude); others: z in [0, 1]
+            const double a = sphere ? -M_PI / 2 : 0.0, b = sphere ? M_PI / 2 : 1.0;
+            const double h = (b - a) / NZ;
+            const double u = a + h * (iz + 0.5 + 0.5 * gx[q]);
+            const double wz = 0.5 * h * gw[q];
+            for (int it = 0; it < NT; ++it) {
+                const double th = 2.0 * M_PI * it / NT;
+                const double c = std::cos(th), s = std::sin(th);
+                double du[3], dt[3], v[3];
+                if (sphere) {
+                    const double cu = std::cos(u), su = std::sin(u);
+                    v[0] = -cu * s; v[1] = cu * c; v[2] = 0.0;  // d/dtheta
+                    lin(m, v, dt);
+                    v[0] = -su * c; v[1] = -su * s; v[2] = cu;  // d/du
+                    lin(m, v, du);
+                } else {
+                    const double rho = 1.0 + (top - 1.0) * u;
+                    v[0] = -rho * s; v[1] = rho * c; v[2] = 0.0;
+                    lin(m, v, dt);
+                    v[0] = (top - 1.0) * c; v[1] = (top - 1.0) * s; v[2] = 1.0;
+                    lin(m, v, du);
+                }
+                area += wz * (2.0 * M_PI / NT) * cross_norm(dt, du);
+            }
+        }
+    return area;
+}
+
+}  // namespace
+
+rf_status rf_surface_areas(const rf_primitive *prims, int32_t n, double *areas)
+{
+    if (!prims || n <= 0 || !areas) return RF_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) {
+        const rf_primitive &p = prims[i];
+        if (p.type < 0 || p.type > RF_DISC || !finite_all(p.m, 12)) return RF_ERR_BAD_SCENE;
+        const double ex[3] = {1, 0, 0}, ey[3] = {0, 1, 0};
+        double mx[3], my[3];
+        lin(p.m, ex, mx);
+        lin(p.m, ey, my);
+        const double plane = cross_norm(mx, my);  // area scale of the plane z = 0
+        switch (p.type) {
+        case RF_DISC: areas[i] = M_PI * plane; break;
+        case RF_ANNULUS: areas[i] = M_PI * std::max(0.0, (double)p.util2 - (double)p.util1) * plane; break;
+        case RF_RECTANGLE: areas[i] = 4.0 * plane; break;
+        case RF_CYLINDER: areas[i] = revolution_area(p.m, 1.0, false); break;
+        case RF_FRUSTUM: areas[i] = revolution_area(p.m, p.util1, false); break;
+        default: areas[i] = revolution_area(p.m, 1.0, true); break;
+        }
+    }
+    return RF_OK;
+}
+
+rf_status rf_budgets_by_area(const rf_primitive *prims, int32_t n, int64_t total_rays, int64_t *rays_out)
+{
+    if (!prims || n <= 0 || !rays_out || total_rays < 0) return RF_ERR_INVALID_ARG;
+    if (total_rays > (kMaxRaysPerEmitter / 2)) return RF_ERR_OVERFLOW;
+    std::vector<double> a(n);
+    rf_status s = rf_surface_areas(prims, n, a.data());
+    if (s != RF_OK) return s;
+    double tot = 0.0;
+    for (double v : a) tot += v;
+    if (!(tot > 0.0)) return RF_ERR_BAD_SCENE;
+    for (int i = 0; i < n; ++i) {
+        const int64_t r = (int64_t)std::llround((double)total_rays * a[i] / tot / 4.0) * 4;
+        rays_out[i] = (a[i] > 0.0 && total_rays > 0) ? std::max<int64_t>(4, r) : 0;
+    }
+    return RF_OK;
 }
 
 rf_status rf_write_output_txt(const char *path, const double *F, int32_t n)

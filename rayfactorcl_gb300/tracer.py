@@ -101,6 +101,26 @@ class Tracer:
         self._keep = self._rays(rays)
         self._check(self._L.rf_trace_async(self._h, ptr(self._keep), 1 if use_bv else 0))
 
+    def trace_range(self, first_ray, count, use_bv: bool = False, accumulate: bool = False):
+        """Trace rays [first, first+count) of every emitter into the running tallies."""
+        f, c = self._rays(first_ray), self._rays(count)
+        self._keep = (f, c)
+        self._check(self._L.rf_trace_range(self._h, ptr(f), ptr(c), 1 if use_bv else 0,
+                                           1 if accumulate else 0))
+
+    def set_tallies(self, hits: np.ndarray, rays):
+        """Restore a checkpoint (tallies and rays traced per emitter)."""
+        h = np.ascontiguousarray(hits, np.uint64)
+        r = self._rays(rays)
+        self._check(self._L.rf_set_tallies(self._h, ptr(h), ptr(r)))
+
+    def results(self):
+        """(int64 tallies, F) of everything traced so far."""
+        hits = np.zeros((self.n, self.n), np.uint64)
+        F = np.zeros((self.n, self.n), np.float64)
+        self._check(self._L.rf_read_results(self._h, ptr(hits), ptr(F)))
+        return hits.astype(np.int64), F
+
     def read_results(self, hits: np.ndarray | None = None, F: np.ndarray | None = None):
         self._check(self._L.rf_read_results(self._h, ptr(hits), ptr(F)))
         return hits, F
@@ -220,6 +240,22 @@ def ray_budgets(scene: Scene, n_samples: int, compat: int = 0) -> np.ndarray:
     prims = np.ascontiguousarray(scene.primitives, PRIM_DTYPE)
     out = np.zeros(prims.shape[0], np.int64)
     check(L.rf_ray_budgets(ptr(prims), prims.shape[0], int(n_samples), compat, ptr(out)))
+    return out
+
+
+def surface_areas(scene: Scene) -> np.ndarray:
+    """FP64 area of every primitive under its transform (no GPU needed)."""
+    prims = np.ascontiguousarray(scene.primitives, PRIM_DTYPE)
+    out = np.zeros(prims.shape[0], np.float64)
+    check(_lib.load().rf_surface_areas(ptr(prims), prims.shape[0], ptr(out)))
+    return out
+
+
+def budgets_by_area(scene: Scene, total_rays: int) -> np.ndarray:
+    """total_rays spread over the emitters by area, multiples of four."""
+    prims = np.ascontiguousarray(scene.primitives, PRIM_DTYPE)
+    out = np.zeros(prims.shape[0], np.int64)
+    check(_lib.load().rf_budgets_by_area(ptr(prims), prims.shape[0], int(total_rays), ptr(out)))
     return out
 
 

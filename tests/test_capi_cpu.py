@@ -189,3 +189,22 @@ def test_loader_matches_reference_on_samples(name):
 def test_cli_reports_missing_file(built_lib, tmp_path, capsys):
     from rayfactorcl_gb300.__main__ import main
     assert main([str(tmp_path / "missing.xml")]) == 1
+
+
+def test_surface_areas_and_area_budgets(built_lib):
+    import math
+    from rayfactorcl_gb300 import generators
+    from rayfactorcl_gb300.tracer import budgets_by_area, surface_areas
+    for w in (generators.enclosure3(), generators.mixed_scene(seed=2), generators.furnace_scene()):
+        a = surface_areas(w.scene)
+        assert np.allclose(a, w.areas, rtol=5e-6)
+        b = budgets_by_area(w.scene, 10**9)
+        assert np.all(b % 4 == 0) and abs(int(b.sum()) - 10**9) < 4 * w.scene.n
+        assert np.allclose(b / b.sum(), a / a.sum(), atol=1e-8)
+    # an ellipsoid: Knud Thomsen's formula (Scene.cpp:373-374) is within 1.061 %
+    xml = """<project><settings><globalRayDensity value="1" /></settings><geometry>
+        <primitive type="sphere"><scale x="1" y="2" z="3" /></primitive></geometry></project>"""
+    sc = parse_scene_xml(xml)
+    p = 1.6075
+    thomsen = 4 * math.pi * ((2 ** p + 3 ** p + 6 ** p) / 3) ** (1 / p)
+    assert abs(surface_areas(sc)[0] / thomsen - 1) < 0.0107

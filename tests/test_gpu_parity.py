@@ -214,3 +214,42 @@ def test_autotune_keeps_results(built_lib, tmp_path, name, prec):
     with _tracer(sc, precision=prec) as t2:
         assert t2.autotune(use_bv=use_bv, cache_path=cache) == cfg
     assert len(cache.read_text().splitlines()) == 1  # served from the cache
+
+
+@pytest.mark.parametrize("prec", [PREC_EXACT, PREC_FAST, "mixed"])
+def test_split_and_resumed_runs_equal_one_run(built_lib, prec):
+    """Checkpoint after a third of the rays, resume in a new context: the tallies and F
+    equal one uninterrupted run (streams depend only on emitter and ray index)."""
+    from rayfactorcl_gb300.tracer import PREC_MIXED
+    prec = PREC_MIXED if prec == "mixed" else prec
+    sc = golden_scene("gen_mixed64")
+    rays = np.full(sc.n, 30001, np.int64)
+    rays[5] = 0
+    with _tracer(sc, precision=prec) as t:
+        full, Ffull = t.trace(rays)
+    part = rays // 3
+    with _tracer(sc, precision=prec) as t:
+        t.trace_range(np.zeros(sc.n, np.int64), part)
+        ck_hits, _ = t.results()
+    with _tracer(sc, precision=prec) as t2:
+        t2.set_tallies(ck_hits, part)
+        t2.trace_range(part, rays - part, accumulate=True)
+        hits, F = t2.results()
+    assert np.array_equal(hits, full)
+    nz = rays > 0
+    assert np.array_equal(F[nz], Ffull[nz])
+
+
+def test_sharded_ranges_sum_to_one_run(built_lib):
+    from rayfactorcl_gb300.shard import shard_ranges
+    sc = golden_scene("gen_sweep2")
+    rays = np.arange(sc.n, dtype=np.int64) * 997 + 5
+    with _tracer(sc) as t:
+        full, _ = t.trace(rays)
+    total = np.zeros_like(full)
+    for r in range(3):
+        first, count = shard_ranges(rays, r, 3)
+        with _tracer(sc) as t:
+            t.trace_range(first, count)
+            total += t.results()[0]
+    assert np.array_equal(total, full)
