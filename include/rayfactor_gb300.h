@@ -222,6 +222,15 @@ rf_status rf_converge_batch(rf_ctx *ctx, const rf_scene_desc *scenes, int32_t n_
 rf_status rf_check_F(rf_ctx *ctx, const double *F, const double *areas, int32_t n,
                      double *max_sum_err, double *max_recip_err);
 
+/* Post-processing of F in FP64 on the device: the closest reciprocal F (A_i F_ij
+ * = A_j F_ji, by symmetrising the exchange matrix A_i F_ij) and, when closed is
+ * set (a closed enclosure), the symmetric scaling of that matrix whose rows sum
+ * to A_i, i.e. sum_j F_ij = 1 with reciprocity kept.  Rows without rays (NaN)
+ * count as zero.  iterations / residual (may be NULL): scaling iterations and
+ * the last max_i |sum_j F_ij - 1|.  F and F_out may be the same array. */
+rf_status rf_smooth_F(rf_ctx *ctx, const double *F, const double *areas, int32_t n, int32_t closed,
+                      double *F_out, int32_t *iterations, double *residual);
+
 /* Pick the launch shape of the single-scene kernels for the current scene by
  * timing runs of about 2^25 rays (spread over the emitters like the budgets of
  * the context's last trace, else evenly) of every combination of threads per block

@@ -1009,6 +1009,38 @@ rf_status rf_check_F(rf_ctx *c, const double *F, const double *areas, int32_t n,
     return RF_OK;
 }
 
+rf_status rf_smooth_F(rf_ctx *c, const double *F, const double *areas, int32_t n, int32_t closed,
+                      double *F_out, int32_t *iterations, double *residual)
+{
+    if (!c || !F || !areas || !F_out || n <= 0) return RF_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i)
+        if (!(areas[i] >= 0.0) || !std::isfinite(areas[i])) return fail(c, RF_ERR_INVALID_ARG, "bad area %d", i);
+    RF_CUDA(c, cudaSetDevice(c->device));
+    const size_t nn = (size_t)n * n;
+    RF_CUDA(c, c->d_F.ensure(nn * sizeof(double)));
+    RF_CUDA(c, c->d_misc.ensure((nn + 4 * (size_t)n + 8) * sizeof(double)));
+    double *d_G = c->d_misc.as<double>();
+    double *d_A = d_G + nn, *d_x0 = d_A + n, *d_x1 = d_x0 + n, *d_out = d_x1 + n, *d_err = d_out + n;
+    // F_out goes through the F buffer: input first, result afterwards
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_F.p, F, nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    RF_CUDA(c, cudaMemcpyAsync(d_A, areas, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    DevBuf out;
+    RF_CUDA(c, out.ensure(nn * sizeof(double)));
+    int it = 0;
+    double err = 0.0;
+    cudaError_t e = launch_smooth(c->d_F.as<double>(), d_A, n, closed ? 1 : 0, 2000, 1e-13, d_G, d_x0, d_x1, d_err,
+                                  out.as<double>(), &it, &err, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F_out, out.p, nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    out.release();
+    (void)d_out;
+    if (e != cudaSuccess) return cuda_fail(c, e, "smoothing");
+    if (iterations) *iterations = it;
+    if (residual) *residual = err;
+    return RF_OK;
+}
+
 rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s)
 {
     if (!fma_per_s) return RF_ERR_INVALID_ARG;

@@ -111,5 +111,8 @@ cudaError_t launch_decide_round(int32_t *flags, int32_t max_rounds, unsigned lon
 cudaError_t launch_check_F(const double *F, const double *areas, int n, double *out2,
                            cudaStream_t st);
 cudaError_t launch_fp32_probe(float *out, int iters, int grid, int block, cudaStream_t st);
+cudaError_t launch_smooth(const double *F, const double *A, int n, int closed, int max_iter, double tol,
+                          double *G, double *x0, double *x1, double *err_dev, double *F_out, int *iters,
+                          double *final_err, cudaStream_t st);
 
 }  // namespace rf

@@ -5,7 +5,10 @@
 // single precision (RayFactorCL/main.cpp:216-249).  Here the 64-bit tallies are
 // normalised in FP64 on the GPU, and the same pass computes each row's largest
 // binomial standard error sqrt(F(1-F)/rays) for the convergence loop.
+#include <algorithm>
 #include <cstdint>
+#include <utility>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "rf_internal.h"
@@ -200,6 +203,94 @@ cudaError_t launch_check_F(const double *F, const double *areas, int n, double *
     cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(double), st);
     if (e != cudaSuccess) return e;
     check_F_kernel<<<n, 256, 0, st>>>(F, areas, n, out2);
+    return cudaGetLastError();
+}
+
+// Reciprocity and summation enforcement (FP64).  G_ij = (A_i F_ij + A_j F_ji)/2
+// is the symmetric exchange matrix closest to the tallies (reciprocity holds
+// exactly for any symmetric G).  For a closed enclosure the rows must also sum
+// to 1: a symmetric scaling X G X with X = diag(x) keeps the symmetry, and x is
+// found by the symmetric Sinkhorn iteration x_i <- sqrt(x_i A_i / (G x)_i).
+__global__ void symmetrise_kernel(const double *F, const double *A, int n, double *G)
+{
+    const int64_t total = (int64_t)n * n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(k / n), j = (int)(k % n);
+        const double a = F[k], b = F[(int64_t)j * n + i];
+        const double fa = (a == a) ? a : 0.0, fb = (b == b) ? b : 0.0;  // rows without rays: 0
+        G[k] = 0.5 * (A[i] * fa + A[j] * fb);
+    }
+}
+
+// one block per row: s_i = sum_j G_ij x_j, then x_i <- sqrt(x_i A_i / s_i);
+// err = max_i |x_i s_i / A_i - 1| before the update
+__global__ void sinkhorn_row_kernel(const double *G, const double *A, int n, const double *x_in, double *x_out,
+                                    double *err)
+{
+    const int i = blockIdx.x;
+    double s = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) s += G[(int64_t)i * n + j] * x_in[j];
+    __shared__ double sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double si = sh[0];
+        if (si > 0.0 && A[i] > 0.0) {
+            x_out[i] = sqrt(x_in[i] * A[i] / si);
+            const double e = fabs(x_in[i] * si / A[i] - 1.0);
+            atomicMax(reinterpret_cast<unsigned long long *>(err), (unsigned long long)__double_as_longlong(e));
+        } else {
+            x_out[i] = x_in[i];  // a surface that sees nothing keeps its row
+        }
+    }
+}
+
+__global__ void scale_out_kernel(const double *G, const double *A, const double *x, int n, int closed, double *F)
+{
+    const int64_t total = (int64_t)n * n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(k / n), j = (int)(k % n);
+        const double g = closed ? x[i] * G[k] * x[j] : G[k];
+        F[k] = A[i] > 0.0 ? g / A[i] : 0.0;
+    }
+}
+
+cudaError_t launch_smooth(const double *F, const double *A, int n, int closed, int max_iter, double tol,
+                          double *G, double *x0, double *x1, double *err_dev, double *F_out, int *iters,
+                          double *final_err, cudaStream_t st)
+{
+    const int64_t total = (int64_t)n * n;
+    int grid = (int)std::min<int64_t>(4096, (total + 255) / 256);
+    symmetrise_kernel<<<grid, 256, 0, st>>>(F, A, n, G);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    *iters = 0;
+    *final_err = 0.0;
+    double *xa = x0, *xb = x1;
+    if (closed) {
+        std::vector<double> ones(n, 1.0);
+        if ((e = cudaMemcpyAsync(xa, ones.data(), n * sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return e;
+        for (int it = 0; it < max_iter; ++it) {
+            if ((e = cudaMemsetAsync(err_dev, 0, sizeof(double), st)) != cudaSuccess) return e;
+            sinkhorn_row_kernel<<<n, 256, 0, st>>>(G, A, n, xa, xb, err_dev);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            std::swap(xa, xb);
+            *iters = it + 1;
+            if ((it & 7) == 7 || it + 1 == max_iter) {
+                double h = 0.0;
+                if ((e = cudaMemcpyAsync(&h, err_dev, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+                if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+                *final_err = h;
+                if (h <= tol) break;
+            }
+        }
+    }
+    scale_out_kernel<<<grid, 256, 0, st>>>(G, A, xa, n, closed, F_out);
     return cudaGetLastError();
 }
 

@@ -225,6 +225,16 @@ class Tracer:
             off += n
         return self._split(scenes, hits.astype(np.int64)), self._split(scenes, F), rl, rounds.value
 
+    def smooth_F(self, F: np.ndarray, areas: np.ndarray, closed: bool = True):
+        """Reciprocity (and, for a closed enclosure, summation) enforced in FP64."""
+        F = np.ascontiguousarray(F, np.float64)
+        a = np.ascontiguousarray(areas, np.float64)
+        out = np.zeros_like(F)
+        it, res = ctypes.c_int32(), ctypes.c_double()
+        self._check(self._L.rf_smooth_F(self._h, ptr(F), ptr(a), F.shape[0], 1 if closed else 0, ptr(out),
+                                        ctypes.byref(it), ctypes.byref(res)))
+        return out, it.value, res.value
+
     def check_F(self, F: np.ndarray, areas: np.ndarray | None = None):
         F = np.ascontiguousarray(F, np.float64)
         a = None if areas is None else np.ascontiguousarray(areas, np.float64)

@@ -253,3 +253,24 @@ def test_sharded_ranges_sum_to_one_run(built_lib):
             t.trace_range(first, count)
             total += t.results()[0]
     assert np.array_equal(total, full)
+
+
+def test_smoothing_enforces_reciprocity_and_summation(built_lib):
+    """FP64 post-processing on the device: reciprocity exact, rows of a closed
+    enclosure sum to one, and the result is no further from the closed form."""
+    from rayfactorcl_gb300.tracer import surface_areas
+    sc = gen_scene("gen_enclosure3")
+    a = surface_areas(sc)
+    assert np.allclose(a, [np.pi * 0.25, np.pi * 0.25, np.pi], rtol=1e-6)
+    n_rays = 2_000_000
+    with _tracer(sc, key1=3) as t:
+        _, F = t.trace(np.full(3, n_rays))
+        Fs, it, res = t.smooth_F(F, a, closed=True)
+        Fo, _, _ = t.smooth_F(F, a, closed=False)
+    AF = a[:, None] * Fs
+    assert np.max(np.abs(AF - AF.T)) < 1e-12
+    assert np.max(np.abs(Fs.sum(axis=1) - 1)) < 1e-10 and res < 1e-10 and it >= 1
+    AFo = a[:, None] * Fo
+    assert np.max(np.abs(AFo - AFo.T)) < 1e-12
+    ref = analytic.enclosure3()
+    assert np.max(np.abs(Fs - ref)) <= np.max(np.abs(F - ref)) + 2e-4
