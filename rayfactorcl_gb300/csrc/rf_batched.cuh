@@ -478,18 +478,31 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
 #pragma unroll 1
                     for (int w = 0; w < nwords; ++w) {
                         unsigned cm = __shfl_sync(0xffffffffu, cmask, w);
+                        // two candidates per pass: their sphere checks are independent
+                        // chains (latency hidden); tests still run in index order
                         while (cm) {
-                            const int j = j0 + (w << 5) + __ffs(cm) - 1;
+                            const int ja = j0 + (w << 5) + __ffs(cm) - 1;
                             cm &= cm - 1;
-                            const float4 bsj = resident ? S.bs[j] : __ldg(gbs + j);
-                            if (!__any_sync(0xffffffffu, valid && ray_may_hit(ray, idd, bsj))) continue;
-                            const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
-                            const int type = __float_as_int(h.aux.x);
-                            if (lane == 0 && (unsigned)type < 6u) S.wcount[warp][type] += nvalid;
-                            bool defer = false;
-                            const float t = hit_mixed(type, h, ray, eps, sc, defer);
-                            if (t < tb) { tb = t; bi = j; }
-                            dj = defer ? (dj == -1 ? j : -2) : dj;  // predicated, no branch
+                            const int jb = cm ? j0 + (w << 5) + __ffs(cm) - 1 : -1;
+                            if (cm) cm &= cm - 1;
+                            const float4 ba = resident ? S.bs[ja] : __ldg(gbs + ja);
+                            const float4 bb = resident ? S.bs[jb >= 0 ? jb : ja] : __ldg(gbs + (jb >= 0 ? jb : ja));
+                            const bool ma = valid && ray_may_hit(ray, idd, ba);
+                            const bool mb = valid && jb >= 0 && ray_may_hit(ray, idd, bb);
+                            const unsigned va = __ballot_sync(0xffffffffu, ma);
+                            const unsigned vb = __ballot_sync(0xffffffffu, mb);
+#pragma unroll
+                            for (int q = 0; q < 2; ++q) {
+                                const int j = q ? jb : ja;
+                                if (!(q ? vb : va)) continue;  // warp-uniform
+                                const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
+                                const int type = __float_as_int(h.aux.x);
+                                if (lane == 0 && (unsigned)type < 6u) S.wcount[warp][type] += nvalid;
+                                bool defer = false;
+                                const float t = hit_mixed(type, h, ray, eps, sc, defer);
+                                if (t < tb) { tb = t; bi = j; }
+                                dj = defer ? (dj == -1 ? j : -2) : dj;  // predicated, no branch
+                            }
                         }
                     }
                 }
