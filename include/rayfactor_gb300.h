@@ -206,8 +206,10 @@ rf_status rf_trace_batch(rf_ctx *ctx, const rf_scene_desc *scenes, int32_t n_sce
                          uint64_t *hits_out, double *F_out);
 
 /* Convergence loop: add rays to every emitter whose row still has a binomial
- * standard error sqrt(F(1-F)/rays) above tol, in rounds of round_rays per
- * emitter, until every row is below tol or max_rounds rounds ran.  The round is
+ * standard error sqrt(F(1-F)/rays) above tol, until every row is below tol or
+ * max_rounds rounds ran.  Each round gives such a row the rays its current
+ * estimate still needs, ceil(max_j F(1-F)/tol^2) - rays rounded up to a
+ * multiple of 4, but at most round_rays (and at least 4).  The round is
  * a CUDA graph (trace + FP64 normalisation + convergence test) replayed by a
  * device-side loop.  rays_out (sum n_i, may be NULL) gets the final budgets;
  * rounds_out the rounds run. */

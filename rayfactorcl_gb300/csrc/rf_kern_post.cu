@@ -39,7 +39,10 @@ cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_
 }
 
 // One warp per row of the batched tally: F, row standard error and the next
-// round's budget.  A row converges when max_j sqrt(F(1-F)/rays) <= tol.
+// round's budget.  A row converges when max_j sqrt(F(1-F)/rays) <= tol.  An
+// unconverged row is given the rays its current estimate says it still needs,
+// ceil(max_j F(1-F) / tol^2) - rays (rounded up to whole draws of 4 rays), at
+// most round_rays per round; an underestimate is corrected by the next round.
 __global__ void converge_step_kernel(const unsigned long long *hits, int64_t *rays,
                                      const int64_t *row_off, const int32_t *row_n, int64_t nrows,
                                      double *F, double tol, int64_t *next_rays, int64_t round_rays,
@@ -51,17 +54,24 @@ __global__ void converge_step_kernel(const unsigned long long *hits, int64_t *ra
     const int64_t off = row_off[warp];
     const int len = row_n[warp];
     const int64_t r = rays[warp];
-    double worst = 0.0;
+    double worst = 0.0;  // max_j F(1-F)
     for (int j = lane; j < len; j += 32) {
         const double f = r > 0 ? (double)hits[off + j] / (double)r : 0.0;
         if (F) F[off + j] = r > 0 ? f : __longlong_as_double(0x7ff8000000000000ll);
-        const double var = r > 0 ? f * (1.0 - f) / (double)r : 1.0;
-        worst = fmax(worst, var);
+        worst = fmax(worst, r > 0 ? f * (1.0 - f) : 1.0);
     }
     for (int o = 16; o; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
     if (lane == 0) {
-        const bool more = sqrt(worst) > tol;
-        next_rays[warp] = more ? round_rays : 0;
+        const bool more = r <= 0 || sqrt(worst / (double)r) > tol;
+        int64_t add = 0;
+        if (more) {
+            const double need = r > 0 ? ceil(worst / (tol * tol)) - (double)r : (double)round_rays;
+            add = need >= (double)round_rays ? round_rays : (int64_t)need;
+            add = (add + 3) & ~(int64_t)3;
+            if (add < 4) add = 4;
+            if (add > round_rays) add = round_rays;
+        }
+        next_rays[warp] = add;
         if (more) atomicAdd(not_converged, 1);
     }
 }

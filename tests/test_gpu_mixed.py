@@ -128,13 +128,16 @@ def test_convergence_loop(built_lib):
     tol = 2e-3
     with Tracer(precision=PREC_MIXED) as t:
         hits, F, rays, rounds = t.converge_batch(scenes, init, tol=tol, round_rays=20480, max_rounds=64)
-    assert 1 <= rounds < 64
+    assert 1 <= rounds < 16
     for sc, h, f, r in zip(scenes, hits, F, rays):
         assert np.all(r >= 4096)
         sig = np.sqrt(f * (1 - f) / r[:, None])
         assert np.all(sig.max(axis=1) <= tol + 1e-12)
-        # rows stop as soon as they converge: one round fewer would not have sufficed
-        assert np.all((r - 4096) % 20480 == 0)
+        # rows are given what their estimate still needs (at most 20480 per round), so
+        # a row ends near max_j F(1-F)/tol^2 rays instead of a whole round beyond it
+        need = (f * (1 - f)).max(axis=1) / tol ** 2
+        assert np.all(r % 4 == 0)
+        assert np.all(r <= np.maximum(4096, 1.25 * need + 4096))
     with Tracer(precision=PREC_MIXED) as t:
         h2, F2 = t.trace_batch(scenes, rays)
     for a, b in zip(hits, h2):
