@@ -110,7 +110,12 @@ def dist_info():
 
 def workload(args):
     from rayfactorcl_gb300 import generators
-    return generators.mixed_scene(seed=2, total_rays=args.rays)
+    if args.surfaces == 64:
+        return generators.mixed_scene(seed=2, total_rays=args.rays)
+    frac = np.array([16, 16, 12, 10, 10], float) / 64.0
+    counts = np.floor(frac * args.surfaces).astype(int)
+    counts[0] += args.surfaces - counts.sum()
+    return generators.mixed_scene(seed=2, total_rays=args.rays, counts=tuple(int(c) for c in counts))
 
 
 def cpu_rate(w, seconds: float, threads: int = 0):
@@ -325,8 +330,10 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "mixed64 seed 2: 64 surfaces (16 cyl, 16 frustum, 12 disc, 10 annulus, "
-                               "10 sphere), 1e8 rays/step spread by area",
+        "config": {"workload": ("mixed64 seed 2: 64 surfaces (16 cyl, 16 frustum, 12 disc, 10 annulus, "
+                                "10 sphere), 1e8 rays/step spread by area") if args.surfaces == 64 else
+                               f"mixed scene seed 2: {args.surfaces} surfaces (mixed64 type mix), "
+                               f"{args.rays:.0e} rays/step spread by area",
                    "kernel": kname, "l2": "flushed between steps (256 MB write)",
                    "rays_per_step": total_rays},
         "e2e": {"value": world * total_rays / (float(np.mean(e2e_ms)) * 1e-3), "unit": "rays/s",
@@ -361,7 +368,7 @@ def run_sweep(args):
     import torch
 
     from rayfactorcl_gb300 import _lib, generators
-    from rayfactorcl_gb300.tracer import PREC_MIXED, Tracer
+    from rayfactorcl_gb300.tracer import PREC_EXACT, PREC_MIXED, Tracer
 
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
@@ -379,6 +386,21 @@ def run_sweep(args):
             dt = time.perf_counter() - t0
         ms, launches = t.last_stats()
         refined = t.refined_count()
+        # the plain kernel against the batched kernel on identical rays: every
+        # 16th scene with 1/64 of its converged budgets
+        sub = list(range(0, len(scenes), 16))
+        sub_rays = [np.maximum(rays[i] // 64 // 4 * 4, 4) for i in sub]
+        sub_scenes = [scenes[i] for i in sub]
+        n_sub = int(sum(int(r.sum()) for r in sub_rays))
+        t.trace_batch(sub_scenes, sub_rays)
+        b_ms = t.last_stats()[0]
+    p_ms = 0.0
+    for sc, r in zip(sub_scenes, sub_rays):
+        with Tracer(precision=PREC_EXACT, device=local) as tp:
+            tp.set_scene(sc)
+            tp.trace(r)  # warm-up
+            tp.trace(r)
+            p_ms += tp.last_stats()[0]
     total = int(sum(int(r.sum()) for r in rays))
     worst = max(float(np.sqrt(np.clip(f * (1 - f), 0, None) / r[:, None]).max()) for f, r in zip(F, rays))
     line = {"metric": METRIC, "value": total / (ms * 1e-3), "unit": "rays/s", "n_gpus": 1, "steps": 1,
@@ -388,6 +410,9 @@ def run_sweep(args):
                                    f"budgets 1e5-1e7, convergence to std err <= {args.sweep_tol}",
                        "kernel": "batched mixed-precision persistent kernel in a CUDA-graph while loop"},
             "rays_total": total, "rounds": rounds, "max_std_err": worst, "wall_s": dt,
+            "plain_subset": {"scenes": len(sub), "rays": n_sub, "surfaces": [int(sc.n) for sc in sub_scenes],
+                             "batched_rays_per_s": n_sub / (b_ms * 1e-3),
+                             "plain_rays_per_s": n_sub / (p_ms * 1e-3), "speedup": p_ms / b_ms},
             "gpu_launches": launches, "fp64_refined_tests": refined, "clocks": clocks.summary()}
     print(json.dumps(line))
     return 0
@@ -404,6 +429,7 @@ def main():
     ap.add_argument("--no-ferr", action="store_true")
     ap.add_argument("--ferr-div", type=int, default=10)
     ap.add_argument("--rays", type=int, default=100_000_000)
+    ap.add_argument("--surfaces", type=int, default=64, help="surfaces of the mixed scene (same type mix)")
     ap.add_argument("--rays-per-thread", type=int, default=0, choices=[0, 4, 8])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)

@@ -5,22 +5,24 @@
 // emitter) segment; a persistent grid pulls them from a device queue (an
 // atomic counter), so scenes of 10 and of 400 surfaces load-balance.
 //
-// Per chunk a block
-//   1. emits its 4096 rays with FP32 hardware approximations into shared memory
-//      (same streams and emission formulas as the plain kernel,
-//      RayFactorGPU.cl:298-443),
-//   2. counting-sorts them by direction cell (octahedral map, 8x8 cells in
-//      Morton order), so that 32 consecutive rays point roughly the same way,
-//   3. lets its warps take packets of 32 sorted rays from a shared counter.
-//      The packet's origin ball and direction cone are reduced across the
-//      warp; then each lane checks the cone against a different surface's
-//      bounding sphere, 32 surfaces per pass, and a ballot gives the packet's
-//      candidate surfaces.  For each candidate (in index order) every lane
-//      checks its own ray against the sphere, and the full test runs only if
-//      some lane's ray can reach it, so coherent packets skip most surfaces,
+// Per chunk (32768 rays) a block
+//   1. emits every ray with FP32 hardware approximations (same streams and
+//      emission formulas as the plain kernel, RayFactorGPU.cl:298-443) only to
+//      compute its sort key: octahedral direction cell (16x16, Morton order)
+//      above a 4x4 cell of the two surface parameters of the emission point,
+//   2. counting-sorts the ray indices by key in shared memory,
+//   3. lets its warps take packets of 32 sorted rays from a shared counter; each
+//      lane re-emits its ray from the stream (keys and indices are all that a
+//      chunk keeps, so chunks are 8x larger than stored rays would allow and
+//      packets are tighter).  The packet's origin ball and direction cone are
+//      reduced across the warp; then each lane checks the cone against a
+//      different surface's bounding sphere, 32 surfaces per pass, and a ballot
+//      gives the packet's candidate surfaces.  For each candidate (in index
+//      order) every lane checks its own ray against the sphere, and the full
+//      test runs only if some lane's ray can reach it,
 //   4. evaluates the surviving tests in FP32; a quadric whose discriminant
-//      B^2 - AC is within 64 rounding errors of zero (or a cone whose A lost
-//      12 bits) is re-evaluated in FP64 (counted), and
+//      B^2 - AC is within 16 rounding errors of zero (or a cone whose A lost
+//      12 bits) is re-evaluated in FP64 after the packet (counted), and
 //   5. tallies first hits in a shared-memory row histogram flushed as 64-bit
 //      atomics whenever the (scene, emitter) row changes.
 // Skipping a surface whose bounding sphere no ray of the packet can reach does
@@ -33,27 +35,32 @@
 namespace rf {
 
 constexpr int kBatchThreads = 1024;
-constexpr int kBatchDraws = 1;                                   // draws per thread per chunk
-constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 4096
+constexpr int kBatchDraws = 8;                                   // draws per thread per chunk
+constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 32768
 constexpr int kDirGrid = 16;                                     // octahedral direction cells per axis
-constexpr int kCells = kDirGrid * kDirGrid * 4;                  // sort keys: 256 directions x 4 origins
+constexpr int kOrigCells = 16;                                   // emission-parameter cells (4 x 4)
+constexpr int kCells = kDirGrid * kDirGrid * kOrigCells;         // 4096 sort keys
 constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
 constexpr float kCondRel = 16.0f / 8388608.0f;                   // 16 ulps of the terms
 constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
+static_assert(kCells == 4 * kBatchThreads, "the bucket scan gives each thread four buckets");
 
+// Rays are not stored: emission computes each ray's sort key, and the lane that
+// traces a ray re-emits it from its stream (a Philox draw and the emission
+// formulas), so a chunk costs two bytes of key and two of permutation per ray.
 struct BatchSmem {
-    float ray[6][kChunkRays];           // sx sy sz cx cy cz, by local ray index
-    int16_t bi[kChunkRays];             // rank in bucket, then best surface by sorted position
     uint16_t perm[kChunkRays];          // sorted position -> local ray index
-    uint16_t key[kChunkRays];           // sort key, kCells = invalid ray
-    int cnt[kCells + 2];
+    int16_t keyres[kChunkRays];         // sort key by local ray index, then nearest surface by sorted position
+    __align__(16) int cnt[kCells];      // bucket sizes, then running bucket offsets
+    int wsum[kBatchThreads / 32];
     HitRec tab[kBatchTile];
     float4 bs[kBatchTile];              // bounding spheres, squared widened radius in w
     int hist[kBatchHist];
     rf_primitive emit;
     int64_t chunk;
     int next_packet;
+    int n_valid;
     unsigned long long work[8];
     uint32_t wcount[kBatchThreads / 32][8];  // per warp: tests by type, sphere checks, packets
 };
@@ -355,78 +362,81 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     reinterpret_cast<const float *>(p.emit + si.prim_off + sg.emitter)[tid];
             cur_emitter = sg.emitter;
         }
-        for (int i = tid; i <= kCells; i += blockDim.x) S.cnt[i] = 0;
+        for (int i = tid; i < kCells; i += blockDim.x) S.cnt[i] = 0;
         if (tid == 0) S.next_packet = 0;
         __syncthreads();
 
-        // 1. emission (draw d = g*blockDim + tid, ray l = 4d + v)
+        // 1. sort keys (draw d = g*blockDim + tid, ray l = 4d + v): direction cell
+        // (Morton) above the 4 x 4 cell of the surface parameters (r[0], r[1])
         const int64_t gid0 = (sg.ray_begin >> 2) + (c - sg.chunk_begin) * (int64_t)(kBatchThreads * kBatchDraws);
         const uint32_t sid = (p.compat & RF_COMPAT_STREAMS) ? 0u : (p.scene_id + (uint32_t)sg.scene);
-#pragma unroll
+#pragma unroll 1
         for (int g = 0; g < kBatchDraws; ++g) {
             const int d = g * kBatchThreads + tid;
             const int64_t gid = gid0 + d;
+            if (gid * 4 + 3 < sg.ray_begin || gid * 4 >= sg.ray_end) {  // no ray of this draw
+                *reinterpret_cast<uint2 *>(&S.keyres[4 * d]) = make_uint2(0x10001000u, 0x10001000u);  // kCells
+                continue;
+            }
             const uint4 u = stream_bits(p.compat, p.key1, sid, sg.emitter, gid);
             const float uf[4] = {u01(u.x), u01(u.y), u01(u.z), u01(u.w)};
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
                 float r[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int q = (i + v + 1) & 3;
-                    r[i] = q == 0 ? uf[0] : (q == 1 ? uf[1] : (q == 2 ? uf[2] : uf[3]));
-                }
+                for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
                 const Ray<float> ray = emit_ray<MFast>(S.emit, r);
-                const int l = 4 * d + v;
                 const int64_t rid = gid * 4 + v;
                 const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
-                S.ray[0][l] = ray.sx; S.ray[1][l] = ray.sy; S.ray[2][l] = ray.sz;
-                S.ray[3][l] = ray.cx; S.ray[4][l] = ray.cy; S.ray[5][l] = ray.cz;
-                // direction cell (Morton) with the emission quadrant of the
-                // surface parameters (r[0], r[1]) as its two low bits
-                const int key = valid ? (direction_cell(ray.cx, ray.cy, ray.cz) << 2) |
-                                            (r[0] >= 0.5f ? 1 : 0) | (r[1] >= 0.5f ? 2 : 0)
+                const int key = valid ? (direction_cell(ray.cx, ray.cy, ray.cz) << 4) |
+                                            (min(3, (int)(r[0] * 4.0f)) << 2) | min(3, (int)(r[1] * 4.0f))
                                       : kCells;
-                S.key[l] = (uint16_t)key;
-                S.bi[l] = (int16_t)atomicAdd(&S.cnt[key], 1);  // rank within the bucket
+                S.keyres[4 * d + v] = (int16_t)key;
+                if (valid) atomicAdd(&S.cnt[key], 1);
             }
         }
         __syncthreads();
-        // 2. counting sort: exclusive scan of the kCells+1 bucket sizes (warp 0,
-        // kCells/32 consecutive buckets per lane; the invalid bucket goes last)
-        if (warp == 0) {
-            constexpr int per = kCells / 32;
-            int loc[per], sum = 0;
-#pragma unroll
-            for (int i = 0; i < per; ++i) {
-                loc[i] = S.cnt[lane * per + i];
-                sum += loc[i];
-            }
+        // 2. counting sort: block-wide exclusive scan of the bucket sizes (four
+        // consecutive buckets per thread), then each ray claims a slot of its bucket
+        {
+            const int4 c4 = *reinterpret_cast<const int4 *>(&S.cnt[4 * tid]);
+            const int sum = c4.x + c4.y + c4.z + c4.w;
             int incl = sum;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int t = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += t;
             }
-            const int total_valid = __shfl_sync(0xffffffffu, incl, 31);
-            __syncwarp();
-            int run = incl - sum;
+            if (lane == 31) S.wsum[warp] = incl;
+            __syncthreads();
+            if (warp == 0) {
+                const int x = S.wsum[lane];
+                int xi = x;
 #pragma unroll
-            for (int i = 0; i < per; ++i) {
-                S.cnt[lane * per + i] = run;
-                run += loc[i];
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, xi, o);
+                    if (lane >= o) xi += t;
+                }
+                S.wsum[lane] = xi - x;
+                if (lane == 31) S.n_valid = xi;
             }
-            if (lane == 0) S.cnt[kCells] = total_valid;
+            __syncthreads();
+            const int run = S.wsum[warp] + incl - sum;
+            *reinterpret_cast<int4 *>(&S.cnt[4 * tid]) =
+                make_int4(run, run + c4.x, run + c4.x + c4.y, run + c4.x + c4.y + c4.z);
         }
         __syncthreads();
-#pragma unroll
-        for (int g = 0; g < kBatchDraws; ++g)
+#pragma unroll 1
+        for (int g = 0; g < kBatchDraws; ++g) {
+            const int d = g * kBatchThreads + tid;
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
-                const int l = 4 * (g * kBatchThreads + tid) + v;
-                S.perm[S.cnt[S.key[l]] + S.bi[l]] = (uint16_t)l;
+                const int key = S.keyres[4 * d + v];
+                if (key < kCells) S.perm[atomicAdd(&S.cnt[key], 1)] = (uint16_t)(4 * d + v);
             }
+        }
         __syncthreads();
+        const int n_valid = S.n_valid;
 
         // 3-4. warps take packets of 32 sorted rays; 32 surfaces per pass are
         // prefiltered against the packet's cone, candidates get per-ray sphere
@@ -435,21 +445,33 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
         constexpr bool resident = RESIDENT;
         const HitRec *gtab = p.tab + si.prim_off;
         const float4 *gbs = p.bsph + si.prim_off;
+        const int n_packets = (n_valid + 31) >> 5;
         for (;;) {
             int k = 0;
             if (lane == 0) k = atomicAdd(&S.next_packet, 1);
             k = __shfl_sync(0xffffffffu, k, 0);
-            if (k >= kChunkRays / 32) break;  // warp-uniform
+            if (k >= n_packets) break;  // warp-uniform
             const int pos = k * 32 + lane;
-            const int l = S.perm[pos];
-            const bool valid = S.key[l] < kCells;
+            const bool valid = pos < n_valid;
             const unsigned vmask = __ballot_sync(0xffffffffu, valid);
             int bi = -1;
-            if (vmask) {
+            {
                 const int nvalid = __popc(vmask);
+                // re-emit the lane's ray (an invalid lane traces the packet's first ray)
+                const int l = S.perm[valid ? pos : k * 32];
                 Ray<float> ray;
-                ray.sx = S.ray[0][l]; ray.sy = S.ray[1][l]; ray.sz = S.ray[2][l];
-                ray.cx = S.ray[3][l]; ray.cy = S.ray[4][l]; ray.cz = S.ray[5][l];
+                {
+                    const int v = l & 3;
+                    const uint4 u = stream_bits(p.compat, p.key1, sid, sg.emitter, gid0 + (l >> 2));
+                    const float uf[4] = {u01(u.x), u01(u.y), u01(u.z), u01(u.w)};
+                    float r[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int q = (i + v + 1) & 3;
+                        r[i] = q == 0 ? uf[0] : (q == 1 ? uf[1] : (q == 2 ? uf[2] : uf[3]));
+                    }
+                    ray = emit_ray<MFast>(S.emit, r);
+                }
                 const float idd = 1.0f / (ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
                 float tb = MFast::inf();
                 int dj = -1;  // deferred FP64 test of this lane: surface, or -2 for more than one
@@ -518,7 +540,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     nref += 2;
                 }
             }
-            S.bi[pos] = (int16_t)bi;
+            S.keyres[pos] = (int16_t)bi;
         }
         __syncwarp();
         if (lane < 8) {
@@ -528,12 +550,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
         }
         __syncthreads();
         // 5. tally (or record) by sorted position; all rays of the chunk share one row
-        for (int pos = tid; pos < kChunkRays; pos += blockDim.x) {
-            const int l = S.perm[pos];
-            const bool valid = S.key[l] < kCells;
-            const int h = valid ? S.bi[pos] : -1;
+        const int n_tally = (n_valid + 31) & ~31;  // whole warps (warp_tally needs every lane)
+        for (int pos = tid; pos < n_tally; pos += blockDim.x) {
+            const bool valid = pos < n_valid;
+            const int h = valid ? S.keyres[pos] : -1;
             if (REC) {
-                if (valid) p.rec[gid0 * 4 + l - p.rec_base] = h;
+                if (valid) p.rec[gid0 * 4 + S.perm[pos] - p.rec_base] = h;
             } else if (hist_on) {
                 warp_tally(S.hist, h);
             } else {

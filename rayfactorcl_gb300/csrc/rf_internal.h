@@ -91,7 +91,7 @@ cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, int gr
 int batched_blocks_per_sm(bool rec, bool resident);
 size_t batched_smem_bytes();
 int batched_tile();  // scenes with at most this many surfaces use the resident kernel
-constexpr int kBatchChunkDraws = 1024;  // Philox draws per chunk of the batched kernel
+constexpr int kBatchChunkDraws = 8192;  // Philox draws per chunk of the batched kernel
 
 // Host preparation of one scene for the batched kernel (rf_capi.cu).
 void prepare_mixed_tables(const rf_primitive *prims, int n, rf_primitive *emit, HitRec *tab, float4 *bs);
