@@ -108,14 +108,42 @@ def dist_info():
     return rank, world, local
 
 
+WORKLOADS = {
+    "enclosure3": "3-surface closed enclosure (coaxial discs r=0.5 h=1, inward cylinder), 1e7 rays per surface",
+    "furnace": "furnace-like enclosure: 180 wall rings, 2x20 annuli, fibre, 30-frustum neck-down, one bounding "
+               "cylinder; 1e9 rays spread by area (plain kernel: bounding-surface path)",
+    "stress": "precision stress: thin annuli (0.999), 89.9 degree frusta, unit primitives 1e4 from the origin; "
+              "1e8 rays spread by area",
+}
+
+
 def workload(args):
     from rayfactorcl_gb300 import generators
+    if args.workload == "enclosure3":
+        return generators.enclosure3()
+    if args.workload == "furnace":
+        return generators.furnace_scene()
+    if args.workload == "stress":
+        return generators.precision_stress()
     if args.surfaces == 64:
         return generators.mixed_scene(seed=2, total_rays=args.rays)
     frac = np.array([16, 16, 12, 10, 10], float) / 64.0
     counts = np.floor(frac * args.surfaces).astype(int)
     counts[0] += args.surfaces - counts.sum()
     return generators.mixed_scene(seed=2, total_rays=args.rays, counts=tuple(int(c) for c in counts))
+
+
+def flipped_rows(scene) -> np.ndarray:
+    """Planar emitters (rectangle, disc, annulus) whose FP32 world normal is -z
+    to within rounding."""
+    out = np.zeros(scene.n, bool)
+    for i, pr in enumerate(scene.primitives):
+        if int(pr["type"]) not in (3, 4, 5):
+            continue
+        im = pr["invm"].astype(np.float32).reshape(3, 4)
+        nrm = im[:, 2] / np.float32(np.sqrt(np.sum(im[:, 2].astype(np.float64) ** 2)))
+        out[i] = float(nrm[2]) < -1.0 + 1e-6
+    return out
 
 
 def cpu_rate(w, seconds: float, threads: int = 0):
@@ -168,12 +196,12 @@ def run_reference(args):
     return 0
 
 
-def time_trace(t, rays, steps, warmup, l2_flush, stream):
+def time_trace(t, rays, steps, warmup, l2_flush, stream, use_bv=False):
     """Per-step device time (CUDA events on the library's stream, L2 flushed
     before each step) and the tracing kernel's own time."""
     import torch
     for _ in range(warmup):
-        t.trace_async(rays)
+        t.trace_async(rays, use_bv)
         torch.cuda.synchronize()
     step_ms, kern_ms = [], []
     for _ in range(steps):
@@ -182,7 +210,7 @@ def time_trace(t, rays, steps, warmup, l2_flush, stream):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-        t.trace_async(rays)
+        t.trace_async(rays, use_bv)
         with torch.cuda.stream(stream):
             e1.record(stream)
         e1.synchronize()
@@ -212,6 +240,9 @@ def run_ours(args):
     total_rays = int(rays.sum())
     ref_ops = algorithmic_ops(sc, rays)
     headline = {"mixed": PREC_MIXED, "exact": PREC_EXACT, "fast": PREC_FAST}[args.precision]
+    # the reference traces a scene with bounding surfaces through runBVGPU; the
+    # mixed kernel culls with its own bounding spheres instead
+    plain_bv = bool(sc.use_bounding_volumes) and sc.bounding_volumes is not None and len(sc.bounding_volumes) > 0
 
     fma = ctypes.c_double()
     _lib.check(_lib.load().rf_measure_fp32_peak(local, fma))
@@ -230,14 +261,15 @@ def run_ours(args):
 
     # -- headline kernel: scene resident, per-step device time ------------
     t, stream = tracer(headline)
+    head_bv = plain_bv and headline != PREC_MIXED
     if headline != PREC_MIXED:
-        t.trace_async(rays)
+        t.trace_async(rays, head_bv)
         t.read_results(None, None)
-        t.autotune()
+        t.autotune(head_bv)
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        ms_step, kernel_ms = time_trace(t, rays, args.steps, args.warmup, l2_flush, stream)
+        ms_step, kernel_ms = time_trace(t, rays, args.steps, args.warmup, l2_flush, stream, head_bv)
         torch.cuda.synchronize()
     barrier()
     hits = np.zeros((sc.n, sc.n), np.uint64)
@@ -258,7 +290,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         t.set_scene(sc)
-        t.trace(rays)
+        t.trace(rays, head_bv)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = e2e_ms[args.warmup:]
     h2d = sc.primitives.nbytes + sc.n * 64 + rays.nbytes + 32 * sc.n + 8 * sc.n
@@ -284,10 +316,10 @@ def run_ours(args):
     plain = None
     if headline != PREC_EXACT and not args.no_plain:
         tp, sp = tracer(PREC_EXACT)
-        tp.trace_async(rays)  # the workload's budgets, which the autotuner then tunes for
+        tp.trace_async(rays, plain_bv)  # the workload's budgets, which the autotuner then tunes for
         tp.read_results(None, None)
-        plain_cfg = tp.autotune()  # the plain kernel at its best launch shape
-        p_step, p_kern = time_trace(tp, rays, args.steps, args.warmup, l2_flush, sp)
+        plain_cfg = tp.autotune(plain_bv)  # the plain kernel at its best launch shape
+        p_step, p_kern = time_trace(tp, rays, args.steps, args.warmup, l2_flush, sp, plain_bv)
         tp.close()
         plain = {"value": world * total_rays / (p_step * 1e-3), "unit": "rays/s", "ms_per_step": p_step,
                  "kernel_ms": p_kern, "roofline_frac": ref_ops / (p_kern * 1e-3) / peak_ops,
@@ -300,13 +332,20 @@ def run_ours(args):
         Fs = {}
         for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED), ("exact", PREC_EXACT)):
             tt, _ = tracer(prec)
-            Fs[name] = tt.trace(sub)[1]
+            Fs[name] = tt.trace(sub, plain_bv and prec != PREC_MIXED)[1]
             tt.close()
         sig = np.sqrt(np.clip(Fs["fp64"] * (1 - Fs["fp64"]), 0, None) / sub[:, None])
+        # planar emitters facing -z to FP32 precision: the reference's alignRayDirection
+        # switches to its d = 0.5 branch there in FP32 but not in FP64, so the two
+        # trace different (equally valid) rays and their rows differ statistically
+        flip = flipped_rows(sc)
+        keep = ~flip
         ferr = {"rays": int(sub.sum()),
-                "max_abs_mixed_vs_fp64": float(np.max(np.abs(Fs["mixed"] - Fs["fp64"]))),
-                "max_abs_plain_vs_fp64": float(np.max(np.abs(Fs["exact"] - Fs["fp64"]))),
-                "max_binomial_sigma": float(sig.max())}
+                "max_abs_mixed_vs_fp64": float(np.max(np.abs(Fs["mixed"] - Fs["fp64"])[keep])) if keep.any() else None,
+                "max_abs_plain_vs_fp64": float(np.max(np.abs(Fs["exact"] - Fs["fp64"])[keep])) if keep.any() else None,
+                "max_binomial_sigma": float(sig.max()),
+                "rows_excluded_minus_z_emitters": int(flip.sum()),
+                "max_abs_mixed_vs_fp64_all_rows": float(np.max(np.abs(Fs["mixed"] - Fs["fp64"])))}
 
     # -- CPU baseline -----------------------------------------------------
     cpu = None
@@ -330,7 +369,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": ("mixed64 seed 2: 64 surfaces (16 cyl, 16 frustum, 12 disc, 10 annulus, "
+        "config": {"workload": WORKLOADS[args.workload] if args.workload in WORKLOADS else ("mixed64 seed 2: 64 surfaces (16 cyl, 16 frustum, 12 disc, 10 annulus, "
                                 "10 sphere), 1e8 rays/step spread by area") if args.surfaces == 64 else
                                f"mixed scene seed 2: {args.surfaces} surfaces (mixed64 type mix), "
                                f"{args.rays:.0e} rays/step spread by area",
@@ -434,7 +473,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="mixed64", choices=["mixed64", "sweep"])
+    ap.add_argument("--workload", default="mixed64", choices=["mixed64", "sweep", *WORKLOADS])
     ap.add_argument("--sweep-scenes", type=int, default=256)
     ap.add_argument("--sweep-tol", type=float, default=1e-4)
     ap.add_argument("--sweep-round", type=int, default=1 << 26)

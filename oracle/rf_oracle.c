@@ -472,9 +472,12 @@ static v3d d_transform_normal(const float *im, v3d n)
     return w;
 }
 
+/* RFG:87-97 in FP64, with d = 1/(1 + n.z) formed as (1 - n.z)/(n.x^2 + n.y^2)
+ * for a normal facing -z (equal for a unit normal; no cancellation in 1 + n.z,
+ * which near -z leaves d with a few correct bits and biases the directions). */
 static v3d d_align_dir(v3d o, v3d n)
 {
-    double d = 1.0 / (1.0 + n.z);
+    double d = n.z < 0.0 ? (1.0 - n.z) * (1.0 / (n.x * n.x + n.y * n.y)) : 1.0 / (1.0 + n.z);
     if (isinf(d)) d = 0.5;
     v3d w;
     w.x = n.z * o.x + n.y * d * (n.y * o.x - n.x * o.y) + n.x * o.z;

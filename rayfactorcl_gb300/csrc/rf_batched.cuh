@@ -20,9 +20,10 @@
 //      gives the packet's candidate surfaces.  For each candidate (in index
 //      order) every lane checks its own ray against the sphere, and the full
 //      test runs only if some lane's ray can reach it,
-//   4. evaluates the surviving tests in FP32; a quadric whose discriminant
-//      B^2 - AC is within 16 rounding errors of zero (or a cone whose A lost
-//      12 bits) is re-evaluated in FP64 after the packet (counted), and
+//   4. evaluates the surviving tests in FP32, with quadric discriminants in
+//      cancellation-free forms; a discriminant within 16 rounding errors of
+//      its terms (a grazing ray), or a cone whose A lost 12 bits, is
+//      re-evaluated in FP64 after the packet (counted), and
 //   5. tallies first hits in a shared-memory row histogram flushed as 64-bit
 //      atomics whenever the (scene, emitter) row changes.
 // Skipping a surface whose bounding sphere no ray of the packet can reach does
@@ -42,6 +43,7 @@ constexpr int kOrigCells = 16;                                   // emission-par
 constexpr int kCells = kDirGrid * kDirGrid * kOrigCells;         // 4096 sort keys
 constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
+constexpr int kBruteMax = 12;                                    // scenes up to this are not culled
 constexpr float kCondRel = 16.0f / 8388608.0f;                   // 16 ulps of the terms
 constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
 static_assert(kCells == 4 * kBatchThreads, "the bucket scan gives each thread four buckets");
@@ -175,12 +177,16 @@ __device__ __forceinline__ Ray<double> to_f64(const Ray<float> &w)
     return d;
 }
 
-// B^2 - AC within 16 rounding errors of zero (FP32 evaluates it to a few): the sign of the discriminant (hit
-// or miss) and the roots are not resolved in FP32.
-__device__ __forceinline__ bool ill_conditioned(float A, float B, float C)
+// The discriminants are evaluated in forms without the cancellation of B^2 -
+// AC (Lagrange's identity): for the unit cylinder B^2 - AC = A - w^2 with
+// w = (s x c)_z; for the cone u^2 + v^2 - w^2 with u = c_x f_s - s_x f_d,
+// v = c_y f_s - s_y f_d; for the unit sphere |c|^2 - |c x s|^2.  Only a
+// discriminant within 16 rounding errors of its terms (a ray grazing the
+// surface) is left undecided in FP32; mag is the sum of the terms' magnitudes
+// times the magnitudes that rounded in them.
+__device__ __forceinline__ bool ill_conditioned(float d, float mag)
 {
-    const float d = B * B - A * C;
-    return fabsf(d) < kCondRel * (B * B + fabsf(A * C));
+    return fabsf(d) < kCondRel * mag;
 }
 
 __device__ __noinline__ float cylinder_f64(const HitRec &h, const Ray<float> &w, float eps)
@@ -203,12 +209,13 @@ __device__ __forceinline__ float cylinder_mixed(const HitRec &h, const Ray<float
     const Ray<float> o = xfrm_ray<MFast>(h, w);
     const float A = fmaf(o.cx, o.cx, o.cy * o.cy);
     const float B = -fmaf(o.sx, o.cx, o.sy * o.cy);
-    const float C = fmaf(o.sx, o.sx, fmaf(o.sy, o.sy, -1.f));
-    if (ill_conditioned(A, B, C)) {
+    const float wz = fmaf(o.sx, o.cy, -o.sy * o.cx);
+    const float d = fmaf(-wz, wz, A);
+    if (ill_conditioned(d, A + fabsf(wz) * (fabsf(o.sx * o.cy) + fabsf(o.sy * o.cx)))) {
         defer = true;
         return MFast::inf();
     }
-    const float disc = MFast::sqrt(B * B - A * C);
+    const float disc = MFast::sqrt(d);  // NaN for a miss, rejected by the comparisons
     const float ra = MFast::rcp(A);
     return quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
 }
@@ -221,13 +228,19 @@ __device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float>
     const float fstart = (top - 1.f) * o.sz + 1.f;
     const float A = fmaf(o.cx, o.cx, fmaf(o.cy, o.cy, -fdir * fdir));
     const float B = -fmaf(o.sx, o.cx, fmaf(o.sy, o.cy, -fstart * fdir));
-    const float C = fmaf(o.sx, o.sx, fmaf(o.sy, o.sy, -fstart * fstart));
+    const float u = fmaf(o.cx, fstart, -o.sx * fdir);
+    const float v = fmaf(o.cy, fstart, -o.sy * fdir);
+    const float wz = fmaf(o.sx, o.cy, -o.sy * o.cx);
+    const float d = fmaf(u, u, fmaf(v, v, -wz * wz));
+    const float mag = fabsf(u) * (fabsf(o.cx * fstart) + fabsf(o.sx * fdir)) +
+                      fabsf(v) * (fabsf(o.cy * fstart) + fabsf(o.sy * fdir)) +
+                      fabsf(wz) * (fabsf(o.sx * o.cy) + fabsf(o.sy * o.cx));
     const float Aterms = o.cx * o.cx + o.cy * o.cy + fdir * fdir;
-    if (ill_conditioned(A, B, C) || fabsf(A) < kCondA * Aterms) {
+    if (ill_conditioned(d, mag) || fabsf(A) < kCondA * Aterms) {
         defer = true;
         return MFast::inf();
     }
-    const float disc = MFast::sqrt(B * B - A * C);
+    const float disc = MFast::sqrt(d);
     const float ra = MFast::rcp(A);
     return quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
 }
@@ -239,12 +252,17 @@ __device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> 
     const Ray<float> o = xfrm_ray<MFast>(h, w);
     const float A = o.cx * o.cx + o.cy * o.cy + o.cz * o.cz;
     const float B = o.cx * o.sx + o.cy * o.sy + o.cz * o.sz;
-    const float C = o.sx * o.sx + o.sy * o.sy + o.sz * o.sz - 1.0f;
-    if (ill_conditioned(A, B, C)) {
+    const float kx = fmaf(o.cy, o.sz, -o.cz * o.sy);
+    const float ky = fmaf(o.cz, o.sx, -o.cx * o.sz);
+    const float kz = fmaf(o.cx, o.sy, -o.cy * o.sx);
+    const float d2 = A - fmaf(kx, kx, fmaf(ky, ky, kz * kz));
+    const float mag = A + fabsf(kx) * (fabsf(o.cy * o.sz) + fabsf(o.cz * o.sy)) +
+                      fabsf(ky) * (fabsf(o.cz * o.sx) + fabsf(o.cx * o.sz)) +
+                      fabsf(kz) * (fabsf(o.cx * o.sy) + fabsf(o.cy * o.sx));
+    if (ill_conditioned(d2, mag)) {
         defer = true;
         return MFast::inf();
     }
-    const float d2 = B * B - A * C;
     if (!(d2 >= 0.f)) return MFast::inf();
     const float d = MFast::sqrt(d2);
     const float ra = MFast::rcp(A);
@@ -365,11 +383,77 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
         for (int i = tid; i < kCells; i += blockDim.x) S.cnt[i] = 0;
         if (tid == 0) S.next_packet = 0;
         __syncthreads();
+        const int64_t gid0 = (sg.ray_begin >> 2) + (c - sg.chunk_begin) * (int64_t)(kBatchThreads * kBatchDraws);
+        const uint32_t sid = (p.compat & RF_COMPAT_STREAMS) ? 0u : (p.scene_id + (uint32_t)sg.scene);
+        const HitRec *gtab = p.tab + si.prim_off;
+
+        if (si.n <= kBruteMax) {  // block-uniform: too few surfaces for culling to pay
+            // every thread traces its own rays against all surfaces in index order
+            uint32_t nv_warp = 0;
+#pragma unroll 1
+            for (int g = 0; g < kBatchDraws; ++g) {
+                const int d = g * kBatchThreads + tid;
+                const int64_t gid = gid0 + d;
+                const bool any = gid * 4 + 3 >= sg.ray_begin && gid * 4 < sg.ray_end;
+                const uint4 u = any ? stream_bits(p.compat, p.key1, sid, sg.emitter, gid) : make_uint4(0u, 0u, 0u, 0u);
+                const float uf[4] = {u01(u.x), u01(u.y), u01(u.z), u01(u.w)};
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const int64_t rid = gid * 4 + v;
+                    const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
+                    int bi = -1;
+                    if (valid) {
+                        float r[4];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
+                        const Ray<float> ray = emit_ray<MFast>(S.emit, r);
+                        float tb = MFast::inf();
+                        int dj = -1;
+#pragma unroll 1
+                        for (int j = 0; j < si.n; ++j) {
+                            const HitRec h = RESIDENT ? S.tab[j] : load_rec(gtab, j);
+                            bool defer = false;
+                            const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
+                            if (t < tb) { tb = t; bi = j; }
+                            dj = defer ? (dj == -1 ? j : -2) : dj;
+                        }
+                        if (dj >= 0) {
+                            const HitRec hq = RESIDENT ? S.tab[dj] : load_rec(gtab, dj);
+                            const float t = hit_f64(hq, ray, eps, sc);
+                            if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
+                            ++nref;
+                        } else if (dj == -2) {
+                            bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, ray, eps, sc);
+                            nref += 2;
+                        }
+                    }
+                    nv_warp += __popc(__ballot_sync(0xffffffffu, valid));
+                    if (REC) {
+                        if (valid) p.rec[gid0 * 4 + 4 * d + v - p.rec_base] = bi;
+                    } else if (hist_on) {
+                        warp_tally(S.hist, bi);
+                    } else {
+                        warp_tally_global(p.hits + si.hits_off + (int64_t)cur_emitter * si.n, bi);
+                    }
+                }
+            }
+            if (lane == 0 && nv_warp)
+                for (int j = 0; j < si.n; ++j) {
+                    const int type = RESIDENT ? __float_as_int(S.tab[j].aux.x) : __float_as_int(__ldg(&gtab[j].aux.x));
+                    if ((unsigned)type < 6u) S.wcount[warp][type] += nv_warp;
+                }
+            __syncwarp();
+            if (lane < 8) {
+                const uint32_t cnt = S.wcount[warp][lane];
+                if (cnt) atomicAdd(&S.work[lane], (unsigned long long)cnt);
+                S.wcount[warp][lane] = 0u;
+            }
+            __syncthreads();
+            continue;
+        }
 
         // 1. sort keys (draw d = g*blockDim + tid, ray l = 4d + v): direction cell
         // (Morton) above the 4 x 4 cell of the surface parameters (r[0], r[1])
-        const int64_t gid0 = (sg.ray_begin >> 2) + (c - sg.chunk_begin) * (int64_t)(kBatchThreads * kBatchDraws);
-        const uint32_t sid = (p.compat & RF_COMPAT_STREAMS) ? 0u : (p.scene_id + (uint32_t)sg.scene);
 #pragma unroll 1
         for (int g = 0; g < kBatchDraws; ++g) {
             const int d = g * kBatchThreads + tid;
@@ -443,7 +527,6 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
         // checks and, if any lane can reach them, the full test (index order, so
         // ties go to the lower index as in RayFactorGPU.cl:463-467)
         constexpr bool resident = RESIDENT;
-        const HitRec *gtab = p.tab + si.prim_off;
         const float4 *gbs = p.bsph + si.prim_off;
         const int n_packets = (n_valid + 31) >> 5;
         for (;;) {

@@ -326,7 +326,11 @@ template <class M>
 __device__ __forceinline__ V3<typename M::T> align_dir(V3<typename M::T> o, V3<typename M::T> n)
 {
     using T = typename M::T;  // RayFactorGPU.cl:87-97
-    T d = M::rcp(T(1) + n.z);
+    // d = 1/(1 + n.z).  The FP64 tracer, which serves as the accuracy reference,
+    // forms it as (1 - n.z)/(n.x^2 + n.y^2) for a normal facing -z: the same value
+    // for a unit normal, without the cancellation in 1 + n.z that leaves a normal
+    // 1e-7 from -z with a few correct bits (a distorted, biased rotation).
+    T d = (M::kF64 && n.z < T(0)) ? (T(1) - n.z) * M::rcp(n.x * n.x + n.y * n.y) : M::rcp(T(1) + n.z);
     if (isinf(d)) d = T(0.5);
     V3<T> w;
     w.x = n.z * o.x + n.y * d * (n.y * o.x - n.x * o.y) + n.x * o.z;
