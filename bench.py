@@ -141,7 +141,7 @@ def flipped_rows(scene) -> np.ndarray:
         if int(pr["type"]) not in (3, 4, 5):
             continue
         im = pr["invm"].astype(np.float32).reshape(3, 4)
-        nrm = im[:, 2] / np.float32(np.sqrt(np.sum(im[:, 2].astype(np.float64) ** 2)))
+        nrm = im[2, :3] / np.float32(np.sqrt(np.sum(im[2, :3].astype(np.float64) ** 2)))  # invm^T (0,0,1)
         out[i] = float(nrm[2]) < -1.0 + 1e-6
     return out
 

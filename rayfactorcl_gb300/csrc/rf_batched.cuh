@@ -106,46 +106,46 @@ struct Packet {
     bool cull;              // false: the cone is too wide to cull with
 };
 
-__device__ __forceinline__ float warp_sum(float v)
+// Warp-wide float minimum / maximum in one instruction (redux.sync .f32,
+// sm_100a and later); every lane gets the same, exact result.
+__device__ __forceinline__ float warp_min(float v)
 {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return __shfl_sync(0xffffffffu, v, 0);  // butterfly sums may differ in the last bit
+    float r;
+    asm volatile("redux.sync.min.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
 }
 __device__ __forceinline__ float warp_max(float v)
 {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ float warp_min(float v)
-{
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
+    float r;
+    asm volatile("redux.sync.max.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
 }
 
-__device__ __forceinline__ Packet packet_bounds(const Ray<float> &r, float idd, bool valid, int nvalid)
+// Bounds of a packet of rays, one per lane (lanes past the end of the chunk
+// repeat the packet's first ray), the same in every lane: the origin ball is
+// centred on the origins' bounding box, the cone axis on the bounding box of
+// the unit directions; radius and half-angle are then exact maxima.
+__device__ __forceinline__ Packet packet_bounds(const Ray<float> &r, float idd)
 {
     Packet pk;
-    const float w = valid ? 1.0f : 0.0f;
-    const float inv_n = 1.0f / (float)nvalid;
-    pk.ox = warp_sum(w * r.sx) * inv_n;
-    pk.oy = warp_sum(w * r.sy) * inv_n;
-    pk.oz = warp_sum(w * r.sz) * inv_n;
+    pk.ox = 0.5f * (warp_min(r.sx) + warp_max(r.sx));
+    pk.oy = 0.5f * (warp_min(r.sy) + warp_max(r.sy));
+    pk.oz = 0.5f * (warp_min(r.sz) + warp_max(r.sz));
     const float dx = r.sx - pk.ox, dy = r.sy - pk.oy, dz = r.sz - pk.oz;
-    pk.rho = sqrtf(warp_max(valid ? dx * dx + dy * dy + dz * dz : 0.0f)) * 1.0001f + 1e-6f;
+    pk.rho = sqrtf(warp_max(dx * dx + dy * dy + dz * dz)) * 1.0001f + 1e-6f;
     const float ilen = sqrtf(idd);
     const float nx = r.cx * ilen, ny = r.cy * ilen, nz = r.cz * ilen;
-    const float ax = warp_sum(w * nx), ay = warp_sum(w * ny), az = warp_sum(w * nz);
+    const float ax = 0.5f * (warp_min(nx) + warp_max(nx));
+    const float ay = 0.5f * (warp_min(ny) + warp_max(ny));
+    const float az = 0.5f * (warp_min(nz) + warp_max(nz));
     const float al = sqrtf(ax * ax + ay * ay + az * az);
-    const bool ok = al > 1e-3f * (float)nvalid;
+    const bool ok = al > 1e-3f;
     const float ial = ok ? 1.0f / al : 0.0f;
     pk.ax = ax * ial;
     pk.ay = ay * ial;
     pk.az = az * ial;
     // widened by 1e-4 for rounding in the normalisations and dot products
-    const float c = warp_min(valid ? nx * pk.ax + ny * pk.ay + nz * pk.az : 1.0f) - 1e-4f;
+    const float c = warp_min(nx * pk.ax + ny * pk.ay + nz * pk.az) - 1e-4f;
     pk.cull = ok && c > 0.0f;  // cones of 90 degrees or wider are not culled
     pk.cos_t = c;
     pk.sin_t = sqrtf(fmaxf(0.0f, 1.0f - c * c));
@@ -209,15 +209,15 @@ __device__ __forceinline__ float cylinder_mixed(const HitRec &h, const Ray<float
     const Ray<float> o = xfrm_ray<MFast>(h, w);
     const float A = fmaf(o.cx, o.cx, o.cy * o.cy);
     const float B = -fmaf(o.sx, o.cx, o.sy * o.cy);
-    const float wz = fmaf(o.sx, o.cy, -o.sy * o.cx);
+    const float pw = o.sy * o.cx;
+    const float wz = fmaf(o.sx, o.cy, -pw);
     const float d = fmaf(-wz, wz, A);
-    if (ill_conditioned(d, A + fabsf(wz) * (fabsf(o.sx * o.cy) + fabsf(o.sy * o.cx)))) {
-        defer = true;
-        return MFast::inf();
-    }
+    const bool ill = ill_conditioned(d, fmaf(2.0f * fabsf(wz), fabsf(wz) + fabsf(pw), A));
     const float disc = MFast::sqrt(d);  // NaN for a miss, rejected by the comparisons
     const float ra = MFast::rcp(A);
-    return quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
+    const float t = quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
+    defer = ill;  // selects, not a branch: the lanes of a warp stay together
+    return ill ? MFast::inf() : t;
 }
 
 __device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float> &w, float eps, bool &defer)
@@ -228,21 +228,23 @@ __device__ __forceinline__ float frustum_mixed(const HitRec &h, const Ray<float>
     const float fstart = (top - 1.f) * o.sz + 1.f;
     const float A = fmaf(o.cx, o.cx, fmaf(o.cy, o.cy, -fdir * fdir));
     const float B = -fmaf(o.sx, o.cx, fmaf(o.sy, o.cy, -fstart * fdir));
-    const float u = fmaf(o.cx, fstart, -o.sx * fdir);
-    const float v = fmaf(o.cy, fstart, -o.sy * fdir);
-    const float wz = fmaf(o.sx, o.cy, -o.sy * o.cx);
+    // each of u, v, w is one product and one fma: rounding below eps (|p| + |x|) for
+    // the product p and result x, so d is off by at most eps (3 (u^2+v^2+w^2) +
+    // 2 (|u||pu| + |v||pv| + |w||pw|))
+    const float pu = o.sx * fdir, pv = o.sy * fdir, pw = o.sy * o.cx;
+    const float u = fmaf(o.cx, fstart, -pu);
+    const float v = fmaf(o.cy, fstart, -pv);
+    const float wz = fmaf(o.sx, o.cy, -pw);
     const float d = fmaf(u, u, fmaf(v, v, -wz * wz));
-    const float mag = fabsf(u) * (fabsf(o.cx * fstart) + fabsf(o.sx * fdir)) +
-                      fabsf(v) * (fabsf(o.cy * fstart) + fabsf(o.sy * fdir)) +
-                      fabsf(wz) * (fabsf(o.sx * o.cy) + fabsf(o.sy * o.cx));
+    const float sq = fmaf(2.0f * wz, wz, d);  // u^2 + v^2 + w^2
+    const float mag = fmaf(3.0f, sq, 2.0f * fmaf(fabsf(u), fabsf(pu), fmaf(fabsf(v), fabsf(pv), fabsf(wz) * fabsf(pw))));
     const float Aterms = o.cx * o.cx + o.cy * o.cy + fdir * fdir;
-    if (ill_conditioned(d, mag) || fabsf(A) < kCondA * Aterms) {
-        defer = true;
-        return MFast::inf();
-    }
+    const bool ill = ill_conditioned(d, mag) || fabsf(A) < kCondA * Aterms;
     const float disc = MFast::sqrt(d);
     const float ra = MFast::rcp(A);
-    return quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
+    const float t = quadric_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps);
+    defer = ill;
+    return ill ? MFast::inf() : t;
 }
 
 __device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> &w, float eps, bool sc,
@@ -256,20 +258,15 @@ __device__ __forceinline__ float sphere_mixed(const HitRec &h, const Ray<float> 
     const float ky = fmaf(o.cz, o.sx, -o.cx * o.sz);
     const float kz = fmaf(o.cx, o.sy, -o.cy * o.sx);
     const float d2 = A - fmaf(kx, kx, fmaf(ky, ky, kz * kz));
-    const float mag = A + fabsf(kx) * (fabsf(o.cy * o.sz) + fabsf(o.cz * o.sy)) +
-                      fabsf(ky) * (fabsf(o.cz * o.sx) + fabsf(o.cx * o.sz)) +
-                      fabsf(kz) * (fabsf(o.cx * o.sy) + fabsf(o.cy * o.sx));
-    if (ill_conditioned(d2, mag)) {
-        defer = true;
-        return MFast::inf();
-    }
-    if (!(d2 >= 0.f)) return MFast::inf();
-    const float d = MFast::sqrt(d2);
+    // near tangency |c x s| ~ |c| while its products are ~|c||s|: rounding in d2 is
+    // below 2 sqrt(3) eps A |s| + eps A
+    const bool ill = ill_conditioned(d2, A * fmaf(4.0f, fabsf(o.sx) + fabsf(o.sy) + fabsf(o.sz), 1.0f));
+    const float d = MFast::sqrt(d2);  // NaN for a miss: both comparisons below fail
     const float ra = MFast::rcp(A);
     const float t1 = (-B - d) * ra, t2 = (-B + d) * ra;
-    if (t1 > eps) return t1;
-    if (t2 > eps) return t2;
-    return MFast::inf();
+    const float t = t1 > eps ? t1 : (t2 > eps ? t2 : MFast::inf());
+    defer = ill;
+    return ill ? MFast::inf() : t;
 }
 
 __device__ __forceinline__ float hit_mixed(int type, const HitRec &h, const Ray<float> &w, float eps,
@@ -567,7 +564,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     const int nwords = min(32, (si.n - j0 + 31) >> 5);
                     unsigned cmask = 0u;
                     {
-                        const Packet pk = packet_bounds(ray, idd, valid, nvalid);
+                        const Packet pk = packet_bounds(ray, idd);
 #pragma unroll 1
                         for (int w = 0; w < nwords; ++w) {
                             const int js = j0 + (w << 5) + lane;
