@@ -347,6 +347,20 @@ def run_ours(args):
                 "rows_excluded_minus_z_emitters": int(flip.sum()),
                 "max_abs_mixed_vs_fp64_all_rows": float(np.max(np.abs(Fs["mixed"] - Fs["fp64"])))}
 
+    # -- the reference's absolute EPS against a scale-relative one (furnace: the
+    #    fibre's radius, 6.25e-5, is far below EPS = 1e-3)
+    eps_cmp = None
+    if args.workload == "furnace" and ferr is not None:
+        tt = Tracer(precision=PREC_MIXED, key1=w.key1, device=local, eps=-1e-6)
+        tt.set_scene(sc)
+        Frel = tt.trace(sub)[1]
+        tt.close()
+        dF = np.abs(Frel - Fs["mixed"])
+        i, j = np.unravel_index(int(np.argmax(dF)), dF.shape)
+        eps_cmp = {"eps_relative": -1e-6, "max_abs_dF_vs_eps_1e-3": float(dF.max()),
+                   "at": [int(i), int(j)], "F_eps_1e-3": float(Fs["mixed"][i, j]), "F_relative": float(Frel[i, j]),
+                   "sigma": float(sig[i, j])}
+
     # -- CPU baseline -----------------------------------------------------
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -388,6 +402,7 @@ def run_ours(args):
         "work_counts": [int(x) for x in work] if work is not None else None,
         "fp64_refined_tests": refined,
         "f_error": ferr,
+        "eps_comparison": eps_cmp,
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
         "gpu_launches": args.steps,

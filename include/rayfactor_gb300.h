@@ -92,7 +92,9 @@ typedef struct rf_config {
     uint32_t compat;      /* RF_COMPAT_* bits                                               */
     uint32_t precision;   /* rf_precision                                                   */
     uint32_t key1;        /* Philox key word 1 (0xdecafbad in RayFactorGPU.cl:486)           */
-    float eps;            /* self-hit threshold on t (1e-3f, RayFactorGPU.cl:7)              */
+    float eps;            /* self-hit threshold on t: >= 0 absolute (1e-3f, RayFactorGPU.cl:7);
+                           * < 0 relative, |eps| x the diagonal of the scene's bounding box
+                           * (per scene in a batch)                                          */
     int32_t device;       /* CUDA device ordinal                                            */
     int32_t block_size;   /* 0: autotuned / built-in default                                */
     int32_t rays_per_thread; /* 0: default; 4 or 8 (one or two Philox draws)                */

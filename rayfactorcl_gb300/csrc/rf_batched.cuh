@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
     BatchSmem &S = *reinterpret_cast<BatchSmem *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool sc = (p.compat & RF_COMPAT_SPHERE) != 0;
-    const float eps = p.eps;
+    float eps = p.eps;  // the current scene's (SceneInfo::eps)
     const int64_t total = p.d_total ? *p.d_total : p.total_chunks;
     const int nseg = p.d_nseg ? *p.d_nseg : p.nseg;
 
@@ -361,6 +361,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
             if (!REC) flush();
             if (sg.scene != cur_scene) {
                 si = p.scenes[sg.scene];
+                eps = si.eps;
                 hist_on = !REC && si.n <= kBatchHist;
                 if (hist_on)
                     for (int i = tid; i < si.n; i += blockDim.x) S.hist[i] = 0;

@@ -87,6 +87,7 @@ struct rf_ctx {
 
     // scene
     int32_t n = 0, nbv = 0;
+    float eps = 1e-3f;  // the scene's self-hit threshold (cfg.eps, or scaled when negative)
     std::vector<rf_primitive> prims;
     DevBuf d_tab, d_emit, d_bvtab, d_bvinfo;
 
@@ -276,7 +277,7 @@ rf_status run_trace(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_ch
     p.compat = c->cfg.compat;
     p.key1 = c->cfg.key1;
     p.scene_id = c->cfg.scene_id;
-    p.eps = c->cfg.eps;
+    p.eps = c->eps;
     p.use_smem_hist = pl.hist ? 1 : 0;
 
     const int arith = arith_of(c);
@@ -364,6 +365,26 @@ void prepare_mixed(const rf_primitive *prims, int n, rf_primitive *emit, HitRec 
     }
 }
 
+// Self-hit threshold of a scene: eps >= 0 is absolute (the reference's 1e-3,
+// RayFactorGPU.cl:7); eps < 0 is relative, |eps| times the diagonal of the box
+// around the surfaces' bounding spheres, so thin surfaces (a fibre of radius
+// 6e-5 under the reference's absolute 1e-3) and large scenes get one threshold
+// scaled to the scene.
+float scene_eps(float eps, const float4 *bs, int n)
+{
+    if (eps >= 0.0f || n <= 0) return eps;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < n; ++i) {
+        const double c[3] = {bs[i].x, bs[i].y, bs[i].z};
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], c[k] - (double)bs[i].w);
+            hi[k] = std::max(hi[k], c[k] + (double)bs[i].w);
+        }
+    }
+    const double dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return (float)(-(double)eps * std::sqrt(dx * dx + dy * dy + dz * dz));
+}
+
 }  // namespace
 
 // Mixed-precision tables of one scene as the batched kernel reads them
@@ -398,6 +419,8 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     for (int s = 0; s < ns; ++s) {
         const int n = scenes[s].n_prims;
         prepare_mixed(scenes[s].prims, n, emit.data() + off, tab.data() + off, bs.data() + off);
+        c->b_info[s].eps = scene_eps(c->cfg.eps, bs.data() + off, n);
+        c->b_info[s].pad = 0;
         for (int i = 0; i < n; ++i) bs[off + i] = widen_sq(bs[off + i]);
         c->b_info[s].n = n;
         c->b_info[s].prim_off = (int32_t)off;
@@ -452,7 +475,7 @@ TraceParams batch_params(rf_ctx *c)
     p.compat = c->cfg.compat;
     p.key1 = c->cfg.key1;
     p.scene_id = c->cfg.scene_id;
-    p.eps = c->cfg.eps;
+    p.eps = c->cfg.eps;  // per scene: SceneInfo::eps
     return p;
 }
 
@@ -553,7 +576,7 @@ rf_status rf_create(rf_ctx **out, const rf_config *cfg)
         c = *cfg;
     }
     if (c.precision > RF_PREC_FP64) return RF_ERR_INVALID_ARG;
-    if (!(c.eps >= 0.0f) || !std::isfinite(c.eps)) return RF_ERR_INVALID_ARG;
+    if (!std::isfinite(c.eps)) return RF_ERR_INVALID_ARG;
     if (c.rays_per_thread != 0 && c.rays_per_thread != 4 && c.rays_per_thread != 8)
         return RF_ERR_INVALID_ARG;
     if (c.block_size < 0 || c.block_size > kBlock || (c.block_size % 32) != 0) return RF_ERR_INVALID_ARG;
@@ -652,6 +675,14 @@ rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf
     c->nbv = nbv;
     c->have_results = false;
     c->b_single = false;
+    c->eps = c->cfg.eps;
+    if (c->cfg.eps < 0.0f) {  // scale-relative: from the scene's bounding spheres
+        std::vector<rf_primitive> e(n);
+        std::vector<HitRec> t(n);
+        std::vector<float4> b(n);
+        prepare_mixed(prims, n, e.data(), t.data(), b.data());
+        c->eps = scene_eps(c->cfg.eps, b.data(), n);
+    }
     if (c->cfg.precision == RF_PREC_MIXED) {
         rf_scene_desc d{prims, n, 0, nullptr};
         if ((st = upload_batch(c, &d, 1, false)) != RF_OK) return st;

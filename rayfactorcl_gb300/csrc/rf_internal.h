@@ -33,6 +33,8 @@ struct SceneInfo {
     int32_t n;           // primitives
     int32_t prim_off;    // first record in the concatenated tables
     int64_t hits_off;    // first tally of its n x n matrix
+    float eps;           // self-hit threshold on t for this scene
+    int32_t pad;
 };
 
 struct TraceParams {

@@ -115,6 +115,7 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     si.n = n;
     si.prim_off = 0;
     si.hits_off = 0;
+    si.eps = eps;
 
     // copies from pageable host memory return once the source has been staged,
     // so the static host tables may be refilled by the next caller

@@ -99,17 +99,20 @@ def _budget_by_area(areas: np.ndarray, total: int) -> np.ndarray:
     return np.maximum(rays, 4)
 
 
-def enclosure3(rays_per_surface: int = 10_000_000, seed: int = 1) -> Workload:
-    x = _Xml("3-surface closed enclosure: coaxial discs r=0.5, h=1, inward cylinder")
-    x.prim("disc", scale=(0.5, 0.5, 1.0))
+def enclosure3(rays_per_surface: int = 10_000_000, seed: int = 1, size: float = 1.0) -> Workload:
+    """Coaxial discs of radius size/2, size apart, closed by an inward cylinder
+    (the view factors do not depend on size)."""
+    h, r = size, 0.5 * size
+    x = _Xml(f"3-surface closed enclosure: coaxial discs r={r:g}, h={h:g}, inward cylinder")
+    x.prim("disc", scale=(r, r, 1.0))
     x.close()
-    x.prim("disc", scale=(0.5, 0.5, 1.0), rotate=(180.0, (1.0, 0.0, 0.0)), translate=(0.0, 0.0, 1.0))
+    x.prim("disc", scale=(r, r, 1.0), rotate=(180.0, (1.0, 0.0, 0.0)), translate=(0.0, 0.0, h))
     x.close()
-    x.prim("cylinderSurface", bounding=True, small=1.0, scale=(0.5, 0.5, 1.0))
+    x.prim("cylinderSurface", bounding=True, small=1.0, scale=(r, r, h))
     x.close()
     text = x.text()
     sc = parse_scene_xml(text)
-    areas = np.array([math.pi * 0.25, math.pi * 0.25, 2 * math.pi * 0.5 * 1.0])
+    areas = np.array([math.pi * r * r, math.pi * r * r, 2 * math.pi * r * h])
     rays = np.full(3, rays_per_surface, np.int64)
     return Workload("enclosure3", text, sc, rays, areas, key1=seed & 0xFFFFFFFF)
 

@@ -124,6 +124,26 @@ def test_enclosure_mixed_analytic(built_lib):
     assert abs(F[0, 1] - ref[0, 1]) < 5 * sig[0, 1] + 3e-4
 
 
+@pytest.mark.parametrize("prec", [PREC_EXACT, PREC_MIXED])
+def test_scale_relative_eps(built_lib, prec):
+    """The enclosure shrunk to 1e-4: under the reference's absolute EPS = 1e-3
+    (RayFactorGPU.cl:7) every hit is nearer than EPS and is dropped; with a negative
+    eps (relative to the scene's extent) the view factors are the closed-form ones,
+    which do not depend on size."""
+    from rayfactorcl_gb300 import generators
+    sc = generators.enclosure3(size=1e-4).scene
+    n = 2_000_000
+    rays = np.full(3, n)
+    with _tracer(sc, precision=prec, key1=1) as t:
+        hits_abs, _ = t.trace(rays)
+    with _tracer(sc, precision=prec, key1=1, eps=-1e-4) as t:
+        _, F = t.trace(rays)
+    assert hits_abs.sum() == 0
+    ref = analytic.enclosure3()
+    sig = binom_sigma(ref, n)
+    assert np.all(np.abs(F - ref) <= 5 * sig + 1e-4), F - ref
+
+
 def test_batch_equals_single_scene_runs(built_lib):
     """Scene s of a batch draws the streams of scene_id = s; each scene's tallies equal a
     single-scene mixed run with that scene_id, whatever the other scenes are."""
