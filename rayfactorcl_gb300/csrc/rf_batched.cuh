@@ -93,8 +93,10 @@ __device__ __forceinline__ bool ray_may_hit(const Ray<float> &r, float idd, cons
 {
     const float ox = b.x - r.sx, oy = b.y - r.sy, oz = b.z - r.sz;
     const float oc2 = ox * ox + oy * oy + oz * oz;
-    const float bb = ox * r.cx + oy * r.cy + oz * r.cz;
-    return oc2 <= b.w || (bb > 0.0f && oc2 - bb * bb * idd <= b.w);
+    const float bb = fmaxf(ox * r.cx + oy * r.cy + oz * r.cz, 0.0f);
+    // origin inside, or the closest approach ahead of the origin is within the
+    // radius (bb = 0 for a sphere behind the origin leaves the first test)
+    return fmaf(-bb * bb, idd, oc2) <= b.w;
 }
 
 // Bounds of a packet of rays (one per lane; invalid lanes excluded), the same
