@@ -81,10 +81,11 @@ __device__ __forceinline__ int direction_cell(float x, float y, float z)
     constexpr float h = 0.5f * kDirGrid;
     const int i = min(kDirGrid - 1, max(0, (int)((u + 1.0f) * h)));
     const int j = min(kDirGrid - 1, max(0, (int)((v + 1.0f) * h)));
-    int m = 0;
-#pragma unroll
-    for (int b = 0; (1 << b) < kDirGrid; ++b) m |= (((i >> b) & 1) << (2 * b)) | (((j >> b) & 1) << (2 * b + 1));
-    return m;
+    static_assert(kDirGrid == 16, "4-bit Morton spread");
+    // spread the 4 bits of i and j to the even / odd bits of an 8-bit code
+    const int si = ((i | (i << 2)) & 0x33) | (((i | (i << 2)) & 0x33) << 1);
+    const int sj = ((j | (j << 2)) & 0x33) | (((j | (j << 2)) & 0x33) << 1);
+    return (si & 0x55) | ((sj & 0x55) << 1);
 }
 
 // Can the ray (origin s, direction c, idd = 1/|c|^2) reach the sphere b?  b.w
@@ -583,17 +584,21 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
 #pragma unroll 1
                     for (int w = 0; w < nwords; ++w) {
                         unsigned cm = __shfl_sync(0xffffffffu, cmask, w);
+                        const int jw = j0 + (w << 5) - 1;
                         // two candidates per pass: their sphere checks are independent
-                        // chains (latency hidden); tests still run in index order
+                        // chains (latency hidden); tests still run in index order.  Lanes
+                        // past the end of the chunk repeat the packet's first ray, so
+                        // their votes change nothing.
                         while (cm) {
-                            const int ja = j0 + (w << 5) + __ffs(cm) - 1;
+                            const int ja = jw + __ffs(cm);
                             cm &= cm - 1;
-                            const int jb = cm ? j0 + (w << 5) + __ffs(cm) - 1 : -1;
-                            if (cm) cm &= cm - 1;
+                            const int jb = cm ? jw + __ffs(cm) : -1;
+                            cm &= cm - 1;  // 0 stays 0
+                            const int jbs = jb >= 0 ? jb : ja;
                             const float4 ba = resident ? S.bs[ja] : __ldg(gbs + ja);
-                            const float4 bb = resident ? S.bs[jb >= 0 ? jb : ja] : __ldg(gbs + (jb >= 0 ? jb : ja));
-                            const bool ma = valid && ray_may_hit(ray, idd, ba);
-                            const bool mb = valid && jb >= 0 && ray_may_hit(ray, idd, bb);
+                            const float4 bb = resident ? S.bs[jbs] : __ldg(gbs + jbs);
+                            const bool ma = ray_may_hit(ray, idd, ba);
+                            const bool mb = jb >= 0 && ray_may_hit(ray, idd, bb);
                             const unsigned va = __ballot_sync(0xffffffffu, ma);
                             const unsigned vb = __ballot_sync(0xffffffffu, mb);
 #pragma unroll
