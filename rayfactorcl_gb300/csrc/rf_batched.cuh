@@ -336,6 +336,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
     if (tid < 8) S.work[tid] = 0ull;
     if (lane < 8) S.wcount[warp][lane] = 0u;
     bool hist_on = false;
+    uint32_t tcount = 0;  // lane t < 6: lane-tests of surfaces of type t by this warp (this chunk)
 
     auto flush = [&]() {
         __syncthreads();
@@ -558,7 +559,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 }
                 const float idd = 1.0f / (ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
                 float tb = MFast::inf();
-                int dj = -1;  // deferred FP64 test of this lane: surface, or -2 for more than one
+                int dj = -1, ndef = 0;  // deferred FP64 tests of this lane: the last one, and how many
                 if (lane == 0) S.wcount[warp][7] += 1;
                 // surfaces in blocks of 1024: phase A tests the packet's cone against 32
                 // spheres per pass and keeps one candidate word per lane; phase B walks the
@@ -607,29 +608,32 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                                 if (!(q ? vb : va)) continue;  // warp-uniform
                                 const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
                                 const int type = __float_as_int(h.aux.x);
-                                if (lane == 0 && (unsigned)type < 6u) S.wcount[warp][type] += nvalid;
+                                tcount += lane == type ? nvalid : 0;
                                 bool defer = false;
                                 const float t = hit_mixed(type, h, ray, eps, sc, defer);
                                 if (t < tb) { tb = t; bi = j; }
-                                dj = defer ? (dj == -1 ? j : -2) : dj;  // predicated, no branch
+                                ndef += defer;  // predicated, no branch
+                                dj = defer ? j : dj;
                             }
                         }
                     }
                 }
                 // the deferred test in FP64 (lower index wins a tie: it ran out of order);
                 // a lane that deferred more than one test re-traces its ray (cold)
-                if (valid && dj >= 0) {
+                if (valid && ndef == 1) {
                     const HitRec hq = RESIDENT ? S.tab[dj] : load_rec(gtab, dj);
                     const float t = hit_f64(hq, ray, eps, sc);
                     if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
                     ++nref;
-                } else if (valid && dj == -2) {
+                } else if (valid && ndef > 1) {
                     bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, ray, eps, sc);
                     nref += 2;
                 }
             }
             S.keyres[pos] = (int16_t)bi;
         }
+        if (lane < 6) S.wcount[warp][lane] += tcount;
+        tcount = 0;
         __syncwarp();
         if (lane < 8) {
             const uint32_t v = S.wcount[warp][lane];
