@@ -70,7 +70,7 @@ struct BatchSmem {
 // Octahedral cell of a direction, kDirGrid x kDirGrid cells in Morton order.
 __device__ __forceinline__ int direction_cell(float x, float y, float z)
 {
-    const float inv = 1.0f / (fabsf(x) + fabsf(y) + fabsf(z) + 1e-30f);
+    const float inv = MFast::rcp(fabsf(x) + fabsf(y) + fabsf(z) + 1e-30f);
     float u = x * inv, v = y * inv;
     if (z < 0.0f) {
         const float uu = (1.0f - fabsf(v)) * copysignf(1.0f, u);
@@ -135,15 +135,17 @@ __device__ __forceinline__ Packet packet_bounds(const Ray<float> &r, float idd)
     pk.oy = 0.5f * (warp_min(r.sy) + warp_max(r.sy));
     pk.oz = 0.5f * (warp_min(r.sz) + warp_max(r.sz));
     const float dx = r.sx - pk.ox, dy = r.sy - pk.oy, dz = r.sz - pk.oz;
-    pk.rho = sqrtf(warp_max(dx * dx + dy * dy + dz * dz)) * 1.0001f + 1e-6f;
-    const float ilen = sqrtf(idd);
+    // hardware square roots and reciprocals (a few ulps): the widening below and
+    // the spheres' 1 % cover them
+    pk.rho = MFast::sqrt(warp_max(dx * dx + dy * dy + dz * dz)) * 1.0001f + 1e-6f;
+    const float ilen = MFast::sqrt(idd);
     const float nx = r.cx * ilen, ny = r.cy * ilen, nz = r.cz * ilen;
     const float ax = 0.5f * (warp_min(nx) + warp_max(nx));
     const float ay = 0.5f * (warp_min(ny) + warp_max(ny));
     const float az = 0.5f * (warp_min(nz) + warp_max(nz));
-    const float al = sqrtf(ax * ax + ay * ay + az * az);
+    const float al = MFast::sqrt(ax * ax + ay * ay + az * az);
     const bool ok = al > 1e-3f;
-    const float ial = ok ? 1.0f / al : 0.0f;
+    const float ial = ok ? MFast::rcp(al) : 0.0f;
     pk.ax = ax * ial;
     pk.ay = ay * ial;
     pk.az = az * ial;
@@ -151,7 +153,7 @@ __device__ __forceinline__ Packet packet_bounds(const Ray<float> &r, float idd)
     const float c = warp_min(nx * pk.ax + ny * pk.ay + nz * pk.az) - 1e-4f;
     pk.cull = ok && c > 0.0f;  // cones of 90 degrees or wider are not culled
     pk.cos_t = c;
-    pk.sin_t = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+    pk.sin_t = MFast::sqrt(fmaxf(0.0f, 1.0f - c * c)) * 1.0001f;
     return pk;
 }
 
@@ -163,11 +165,11 @@ __device__ __forceinline__ bool packet_may_hit(const Packet &pk, const float4 b)
     if (!pk.cull) return true;
     const float vx = b.x - pk.ox, vy = b.y - pk.oy, vz = b.z - pk.oz;
     const float L2 = vx * vx + vy * vy + vz * vz;
-    const float R = sqrtf(b.w) + pk.rho;
+    const float R = MFast::sqrt(b.w) * 1.0001f + pk.rho;
     const float R2 = R * R;
     if (L2 <= R2) return true;
     const float va = vx * pk.ax + vy * pk.ay + vz * pk.az;
-    return va >= pk.cos_t * sqrtf(L2 - R2) - pk.sin_t * R;
+    return va >= pk.cos_t * MFast::sqrt(L2 - R2) - pk.sin_t * R;
 }
 
 // Mixed-precision tests: FP32 with hardware approximations; quadrics whose
@@ -557,7 +559,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     }
                     ray = emit_ray<MFast>(S.emit, r);
                 }
-                const float idd = 1.0f / (ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
+                const float idd = MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
                 float tb = MFast::inf();
                 int dj = -1, ndef = 0;  // deferred FP64 tests of this lane: the last one, and how many
                 if (lane == 0) S.wcount[warp][7] += 1;
