@@ -18,11 +18,22 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "rayfactor_gb300.h"
 #include "rf_internal.h"
 
 using namespace rf;
+
+namespace {
+// NVTX range around an API call (a no-op unless a profiler is attached).
+struct ApiRange {
+    explicit ApiRange(const char *name) { nvtxRangePushA(name); }
+    ~ApiRange() { nvtxRangePop(); }
+    ApiRange(const ApiRange &) = delete;
+    ApiRange &operator=(const ApiRange &) = delete;
+};
+}  // namespace
 
 namespace {
 
@@ -634,6 +645,7 @@ const char *rf_last_error(const rf_ctx *c)
 rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf_bounding_volume *bvs,
                        int32_t nbv)
 {
+    ApiRange nvtx_range("rf_set_scene");
     if (!c) return RF_ERR_INVALID_ARG;
     rf_status st = validate_prims(c, prims, n, 0);
     if (st != RF_OK) return st;
@@ -693,6 +705,7 @@ rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf
 
 rf_status rf_trace_async(rf_ctx *c, const int64_t *rays, int32_t use_bv)
 {
+    ApiRange nvtx_range("rf_trace_async");
     rf_status s = require_scene(c);
     if (s != RF_OK) return s;
     if (!rays) return fail(c, RF_ERR_INVALID_ARG, "rays_per_emitter is NULL");
@@ -725,6 +738,7 @@ rf_status rf_trace_async(rf_ctx *c, const int64_t *rays, int32_t use_bv)
 rf_status rf_trace_range(rf_ctx *c, const int64_t *first_ray, const int64_t *count, int32_t use_bv,
                          int32_t accumulate)
 {
+    ApiRange nvtx_range("rf_trace_range");
     rf_status s = require_scene(c);
     if (s != RF_OK) return s;
     if (!first_ray || !count) return fail(c, RF_ERR_INVALID_ARG, "first_ray / count is NULL");
@@ -780,6 +794,7 @@ rf_status rf_set_tallies(rf_ctx *c, const uint64_t *hits, const int64_t *rays)
 
 rf_status rf_read_results(rf_ctx *c, uint64_t *hits_out, double *F_out)
 {
+    ApiRange nvtx_range("rf_read_results");
     rf_status s = require_scene(c);
     if (s != RF_OK) return s;
     if (!c->have_results) return fail(c, RF_ERR_STATE, "no trace to read");
@@ -817,6 +832,7 @@ rf_status rf_read_results(rf_ctx *c, uint64_t *hits_out, double *F_out)
 
 rf_status rf_trace(rf_ctx *c, const int64_t *rays, int32_t use_bv, uint64_t *hits_out, double *F_out)
 {
+    ApiRange nvtx_range("rf_trace");
     rf_status s = rf_trace_async(c, rays, use_bv);
     if (s != RF_OK) return s;
     return rf_read_results(c, hits_out, F_out);
@@ -1043,6 +1059,7 @@ rf_status rf_check_F(rf_ctx *c, const double *F, const double *areas, int32_t n,
 rf_status rf_smooth_F(rf_ctx *c, const double *F, const double *areas, int32_t n, int32_t closed,
                       double *F_out, int32_t *iterations, double *residual)
 {
+    ApiRange nvtx_range("rf_smooth_F");
     if (!c || !F || !areas || !F_out || n <= 0) return RF_ERR_INVALID_ARG;
     for (int i = 0; i < n; ++i)
         if (!(areas[i] >= 0.0) || !std::isfinite(areas[i])) return fail(c, RF_ERR_INVALID_ARG, "bad area %d", i);
@@ -1112,6 +1129,7 @@ rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s)
 rf_status rf_trace_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_scenes, uint64_t *hits_out,
                          double *F_out)
 {
+    ApiRange nvtx_range("rf_trace_batch");
     if (!c) return RF_ERR_INVALID_ARG;
     rf_status st = upload_batch(c, scenes, n_scenes, true);
     if (st != RF_OK) return st;
@@ -1157,6 +1175,7 @@ rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_sc
                             int64_t round_rays, int32_t max_rounds, uint64_t *hits_out, double *F_out,
                             int64_t *rays_out, int32_t *rounds_out)
 {
+    ApiRange nvtx_range("rf_converge_batch");
     if (!c) return RF_ERR_INVALID_ARG;
     if (!(tol > 0.0) || round_rays <= 0 || max_rounds <= 0)
         return fail(c, RF_ERR_INVALID_ARG, "tol > 0, round_rays > 0 and max_rounds > 0 are required");
@@ -1324,6 +1343,7 @@ void tune_apply(rf_ctx *c, const TuneChoice &t)
 
 rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
 {
+    ApiRange nvtx_range("rf_autotune");
     rf_status s = require_scene(c);
     if (s != RF_OK) return s;
     if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");

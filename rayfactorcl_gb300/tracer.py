@@ -47,6 +47,7 @@ class Tracer:
         self._h = h
         self._L = L
         self.cfg = cfg
+        self.precision = precision
         self.n = 0
         self.scene: Scene | None = None
 
@@ -276,14 +277,21 @@ def write_output_txt(path: str | Path, F: np.ndarray):
 
 
 def run_cl_gpurng(n_samples: int, scene: Scene, output: str | Path | None = "output.txt",
-                  **tracer_kw):
+                  stats: dict | None = None, **tracer_kw):
     """runCL_GPURNG(n_samples, scene) (main.cpp:54-272) on the GPU.
 
     Returns (rays per emitter, int64 tallies, F).  Writes ``output`` unless it is None.
+    ``stats``, if given, receives the tracing kernel's time, its launch count and (mixed
+    precision) the quadric tests re-evaluated in FP64.
     """
     with Tracer(**tracer_kw) as t:
         t.set_scene(scene)
-        rays, hits, F = t.run_gpurng(n_samples, use_bv=bool(scene.use_bounding_volumes))
+        use_bv = bool(scene.use_bounding_volumes) and t.precision != PREC_MIXED
+        rays, hits, F = t.run_gpurng(n_samples, use_bv=use_bv)
+        if stats is not None:
+            ms, launches = t.last_stats()
+            stats.update(kernel_ms=ms, launches=launches,
+                         fp64_refined_tests=t.refined_count() if t.precision == PREC_MIXED else 0)
     if output is not None:
         write_output_txt(output, F)
     return rays, hits, F
