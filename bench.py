@@ -368,6 +368,11 @@ def run_ours(args):
         cpu = {"value": rate, "unit": "rays/s", "cores": nthreads, "kind": "port",
                "sample": f"{sample_rays} rays of the workload, area-weighted, {dt:.1f} s"}
 
+    hbm_peak = None
+    try:
+        hbm_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        hbm_peak = None
     traffic = None
     prof = ROOT / "profiles" / "traffic.json"
     if prof.exists():
@@ -394,7 +399,15 @@ def run_ours(args):
         "roofline": {"bound": "fp32-issue", "achieved": achieved / 1e12, "peak": peak_ops / 1e12,
                      "unit": "Top/s (FP32 ops performed, FMA = 1 op)", "frac": achieved / peak_ops,
                      "traffic": traffic,
-                     "peak_source": "measured in-run: dependent-FMA issue probe (rf_measure_fp32_peak)"},
+                     "peak_source": "measured in-run: dependent-FMA issue probe (rf_measure_fp32_peak)",
+                     # the brute-force work the rays represent (every ray against every
+                     # surface, as the plain kernel does it) per second, against the same peak
+                     "brute_force_equivalent_frac": ref_ops / (kernel_ms * 1e-3) / peak_ops,
+                     # DRAM: the per-launch traffic from ncu over the kernel time, against
+                     # the measured HBM copy bandwidth (the path does not use HBM)
+                     "hbm": ({"achieved_gbs": traffic / (kernel_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
+                              "frac": traffic / (kernel_ms * 1e-3) / 1e9 / hbm_peak}
+                             if traffic and hbm_peak else None)},
         "kernel_ms": kernel_ms,
         "plain_kernel": plain,
         "speedup_vs_plain": (value / plain["value"]) if plain else None,
