@@ -193,7 +193,8 @@ rf_status rf_write_output_txt(const char *path, const double *F, int32_t n);
 /* ---------------------------------------------------------------------------
  * Batched mixed-precision tracing: many independent scenes, many emitters with
  * uneven budgets, one persistent launch that pulls (scene, emitter, ray chunk)
- * work items from a device queue.
+ * work items from a device queue.  A scene has at most 32767 surfaces here
+ * (RF_ERR_OVERFLOW beyond; the plain kernels take any number).
  * ------------------------------------------------------------------------- */
 typedef struct rf_scene_desc {
     const rf_primitive *prims;

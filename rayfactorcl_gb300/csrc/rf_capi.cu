@@ -416,6 +416,9 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     for (int s = 0; s < ns; ++s) {
         rf_status st = validate_prims(c, scenes[s].prims, scenes[s].n_prims, s);
         if (st != RF_OK) return st;
+        if (scenes[s].n_prims > kBatchMaxSurfaces)
+            return fail(c, RF_ERR_OVERFLOW, "scene %d: %d surfaces; the mixed-precision kernel takes at most %d", s,
+                        scenes[s].n_prims, kBatchMaxSurfaces);
         if (with_budgets && !scenes[s].rays_per_emitter)
             return fail(c, RF_ERR_INVALID_ARG, "scene %d: rays_per_emitter is NULL", s);
         nprim += scenes[s].n_prims;

@@ -93,6 +93,7 @@ cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, int gr
 int batched_blocks_per_sm(bool rec, bool resident);
 size_t batched_smem_bytes();
 int batched_tile();  // scenes with at most this many surfaces use the resident kernel
+constexpr int kBatchMaxSurfaces = 32767;  // nearest hits are kept as int16 in shared memory
 constexpr int kBatchChunkDraws = 8192;  // Philox draws per chunk of the batched kernel
 
 // Host preparation of one scene for the batched kernel (rf_capi.cu).

@@ -203,6 +203,11 @@ def test_batch_rejects_bad_input(built_lib):
         with pytest.raises(_lib.RfError) as ei:
             t.trace([4, 4], use_bv=True)
         assert ei.value.status == 8
+        # nearest hits are int16 in the kernel: scenes above 32767 surfaces are refused
+        big = np.repeat(sc.primitives[:1], 32768)
+        with pytest.raises(_lib.RfError) as ei:
+            t.trace_batch([type(sc)(1e6, False, big, sc.bounding_volumes)], [np.zeros(32768, np.int64)])
+        assert _lib.STATUS[ei.value.status] == "RF_ERR_OVERFLOW"
 
 
 def test_mixed_far_offset_self_hits(built_lib, oracle_lib):
