@@ -323,14 +323,27 @@ def run_ours(args):
         tp.close()
         plain = {"value": world * total_rays / (p_step * 1e-3), "unit": "rays/s", "ms_per_step": p_step,
                  "kernel_ms": p_kern, "roofline_frac": ref_ops / (p_kern * 1e-3) / peak_ops,
-                 "launch": plain_cfg}
+                 "launch": plain_cfg, "arithmetic": "bit-exact with the CPU restatement (IEEE rcp/sqrt)"}
+    # the same plain kernel with hardware approximations (the analogue of the
+    # reference's native_* functions): no longer bit-exact, same method
+    plain_fast = None
+    if headline != PREC_FAST and not args.no_plain:
+        tp, sp = tracer(PREC_FAST)
+        tp.trace_async(rays, plain_bv)
+        tp.read_results(None, None)
+        fast_cfg = tp.autotune(plain_bv)
+        f_step, f_kern = time_trace(tp, rays, args.steps, args.warmup, l2_flush, sp, plain_bv)
+        tp.close()
+        plain_fast = {"value": world * total_rays / (f_step * 1e-3), "unit": "rays/s", "ms_per_step": f_step,
+                      "kernel_ms": f_kern, "roofline_frac": ref_ops / (f_kern * 1e-3) / peak_ops,
+                      "launch": fast_cfg, "arithmetic": "FP32 hardware approximations (rcp/sqrt/rsqrt.approx)"}
 
     # -- F error at equal rays against the FP64 tracer (identical streams) ----
     ferr = None
     if not args.no_ferr:
         sub = np.maximum((rays // args.ferr_div) // 4 * 4, 4)
         Fs = {}
-        for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED), ("exact", PREC_EXACT)):
+        for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED), ("exact", PREC_EXACT), ("fast", PREC_FAST)):
             tt, _ = tracer(prec)
             Fs[name] = tt.trace(sub, plain_bv and prec != PREC_MIXED)[1]
             tt.close()
@@ -343,6 +356,7 @@ def run_ours(args):
         ferr = {"rays": int(sub.sum()),
                 "max_abs_mixed_vs_fp64": float(np.max(np.abs(Fs["mixed"] - Fs["fp64"])[keep])) if keep.any() else None,
                 "max_abs_plain_vs_fp64": float(np.max(np.abs(Fs["exact"] - Fs["fp64"])[keep])) if keep.any() else None,
+                "max_abs_plain_fast_vs_fp64": float(np.max(np.abs(Fs["fast"] - Fs["fp64"])[keep])) if keep.any() else None,
                 "max_binomial_sigma": float(sig.max()),
                 "rows_excluded_minus_z_emitters": int(flip.sum()),
                 "max_abs_mixed_vs_fp64_all_rows": float(np.max(np.abs(Fs["mixed"] - Fs["fp64"])))}
@@ -411,6 +425,8 @@ def run_ours(args):
         "kernel_ms": kernel_ms,
         "plain_kernel": plain,
         "speedup_vs_plain": (value / plain["value"]) if plain else None,
+        "plain_kernel_fast": plain_fast,
+        "speedup_vs_plain_fast": (value / plain_fast["value"]) if plain_fast else None,
         "culled_test_fraction": culled,
         "work_counts": [int(x) for x in work] if work is not None else None,
         "fp64_refined_tests": refined,
