@@ -129,7 +129,8 @@ rf_status rf_set_scene(rf_ctx *ctx, const rf_primitive *prims, int32_t n_prims,
 rf_status rf_trace(rf_ctx *ctx, const int64_t *rays_per_emitter, int32_t use_bv,
                    uint64_t *hits_out, double *F_out);
 
-/* Trace rays [first_ray[e], first_ray[e] + count[e]) of every emitter e and add
+/* (No counterpart in the reference, which always starts every emitter at ray 0.)
+ * Trace rays [first_ray[e], first_ray[e] + count[e]) of every emitter e and add
  * the tallies to the context's running tallies (accumulate = 1, after a trace or
  * rf_set_tallies) or start new ones (accumulate = 0).  A ray's stream depends
  * only on (emitter, ray index), so a run split into ranges -- resumed from a
@@ -139,25 +140,28 @@ rf_status rf_trace(rf_ctx *ctx, const int64_t *rays_per_emitter, int32_t use_bv,
 rf_status rf_trace_range(rf_ctx *ctx, const int64_t *first_ray, const int64_t *count,
                          int32_t use_bv, int32_t accumulate);
 
-/* Restore running tallies and ray counts (a checkpoint: n x n tallies and the
+/* (No counterpart in the reference.)
+ * Restore running tallies and ray counts (a checkpoint: n x n tallies and the
  * rays traced per emitter), to continue with rf_trace_range(accumulate = 1). */
 rf_status rf_set_tallies(rf_ctx *ctx, const uint64_t *hits, const int64_t *rays_per_emitter);
 
-/* The same, split for callers that time or overlap the GPU work:
+/* rf_trace split in two (main.cpp:160-234 likewise enqueues, then reads back),
+ * for callers that time or overlap the GPU work:
  * rf_trace_async enqueues on the context's stream and returns; rf_read_results
  * waits and copies the tallies (and F) of the last trace. */
 rf_status rf_trace_async(rf_ctx *ctx, const int64_t *rays_per_emitter, int32_t use_bv);
 rf_status rf_read_results(rf_ctx *ctx, uint64_t *hits_out, double *F_out);
 
-/* The context's CUDA stream (a cudaStream_t), for callers that record their
+/* (No counterpart in the reference.)  The context's CUDA stream (a cudaStream_t), for callers that record their
  * own events or order other work after a trace. */
 void *rf_stream(rf_ctx *ctx);
 
-/* Milliseconds of the last trace's kernels on the device (CUDA events on the
+/* In place of the reference's getticks() prints around enqueue + execute
+ * (main.cpp:156-192): milliseconds of the last trace's kernels on the device (CUDA events on the
  * context's stream) and the number of kernel launches it made. */
 rf_status rf_last_trace_stats(rf_ctx *ctx, double *kernel_ms, int32_t *launches);
 
-/* Per-ray first-hit index (-1 = none) of rays [first_ray, first_ray+n_rays) of
+/* (No counterpart in the reference.)  Per-ray first-hit index (-1 = none) of rays [first_ray, first_ray+n_rays) of
  * one emitter, for parity checks against the CPU restatement. */
 rf_status rf_trace_rays(rf_ctx *ctx, int32_t emitter, int64_t first_ray, int64_t n_rays,
                         int32_t use_bv, int32_t *hit_index_out);
@@ -194,7 +198,9 @@ rf_status rf_write_output_txt(const char *path, const double *F, int32_t n);
  * Batched mixed-precision tracing: many independent scenes, many emitters with
  * uneven budgets, one persistent launch that pulls (scene, emitter, ray chunk)
  * work items from a device queue.  A scene has at most 32767 surfaces here
- * (RF_ERR_OVERFLOW beyond; the plain kernels take any number).
+ * (RF_ERR_OVERFLOW beyond; the plain kernels take any number).  No counterpart
+ * in the reference (one scene per run, main.cpp:275-284), nor for the FP64
+ * checks and smoothing below (the reference writes raw F, main.cpp:236-249).
  * ------------------------------------------------------------------------- */
 typedef struct rf_scene_desc {
     const rf_primitive *prims;
@@ -236,7 +242,8 @@ rf_status rf_check_F(rf_ctx *ctx, const double *F, const double *areas, int32_t 
 rf_status rf_smooth_F(rf_ctx *ctx, const double *F, const double *areas, int32_t n, int32_t closed,
                       double *F_out, int32_t *iterations, double *residual);
 
-/* Pick the launch shape of the single-scene kernels for the current scene by
+/* (No counterpart in the reference, whose work-group size is fixed at 128,
+ * util_opencl.h:52.)  Pick the launch shape of the single-scene kernels for the current scene by
  * timing runs of about 2^25 rays (spread over the emitters like the budgets of
  * the context's last trace, else evenly) of every combination of threads per block
  * (128, 256), rays per thread (4, 8), surface staging (shared-memory tiles or
@@ -247,21 +254,21 @@ rf_status rf_smooth_F(rf_ctx *ctx, const double *F, const double *areas, int32_t
  * Results of a trace do not depend on the launch shape. */
 rf_status rf_autotune(rf_ctx *ctx, int32_t use_bv, const char *cache_path);
 
-/* The launch shape the context uses now (after rf_autotune, or the defaults). */
+/* (No counterpart in the reference.)  The launch shape the context uses now (after rf_autotune, or the defaults). */
 rf_status rf_get_launch_config(rf_ctx *ctx, int32_t *block, int32_t *rays_per_thread,
                                int32_t *smem_hist, int32_t *smem_table);
 
-/* Counters of the last mixed-precision run: tests re-evaluated in FP64. */
+/* (No counterpart in the reference.)  Counters of the last mixed-precision run: tests re-evaluated in FP64. */
 rf_status rf_last_refine_count(rf_ctx *ctx, uint64_t *refined_tests);
 
-/* Work of the last mixed-precision run: counts[0..5] ray x surface tests
+/* (No counterpart in the reference.)  Work of the last mixed-precision run: counts[0..5] ray x surface tests
  * performed by surface type (RF_CYLINDER..RF_DISC), counts[6] candidate
  * surfaces per packet that passed the packet's cone test (each then checked ray
  * by ray), counts[7] ray packets (32 rays).  Tests skipped by culling are the
  * all-pairs count minus the sum of counts[0..5]. */
 rf_status rf_last_work_counts(rf_ctx *ctx, uint64_t *counts);
 
-/* FP32 issue-rate probe: dependent-FMA throughput of the device in FMA/s
+/* (No counterpart in the reference.)  FP32 issue-rate probe: dependent-FMA throughput of the device in FMA/s
  * (one FMA counted as one operation), measured with CUDA events. */
 rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s);
 
