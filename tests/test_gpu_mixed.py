@@ -56,6 +56,53 @@ def test_mixed_per_ray_vs_oracles(built_lib, oracle_lib, name):
     assert bad / total <= 2e-3, (bad, total)
 
 
+def test_mixed_large_scene_through_l1(built_lib, oracle_lib):
+    """A 600-surface scene: too large for the shared-memory tables (512) and row
+    histogram (512), so records and spheres are read through L1 and tallies go
+    to global atomics.  Per-ray hits agree with the oracles and a batch with a
+    small scene equals the single-scene runs."""
+    from rayfactorcl_gb300 import generators
+    sc = generators.mixed_scene(seed=7, total_rays=4, counts=(150, 150, 112, 94, 94)).scene
+    assert sc.n == 600
+    p = O.params(compat=0)
+    total = bad = 0
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        for e in (0, 299, 599):
+            got = t.trace_rays(e, 0, 4096)
+            e64 = O.trace_rays(sc, p, e, 0, 4096, f64=True)
+            e32 = O.trace_rays(sc, p, e, 0, 4096)
+            total += got.size
+            bad += int(np.count_nonzero((got != e64) & (got != e32)))
+    assert bad / total <= 2e-3, (bad, total)
+    small = golden_scene("gen_mixed64")
+    rays = [np.full(sc.n, 5000, np.int64), np.full(small.n, 7000, np.int64)]
+    with Tracer(precision=PREC_MIXED) as t:
+        hits, _ = t.trace_batch([sc, small], rays)
+    for s_id, (scn, r) in enumerate(zip([sc, small], rays)):
+        with _tracer(scn, precision=PREC_MIXED, scene_id=s_id) as t1:
+            h1, _ = t1.trace(r)
+        assert np.array_equal(hits[s_id], h1)
+
+
+@pytest.mark.parametrize("n", [12, 13])
+def test_mixed_brute_force_boundary(built_lib, oracle_lib, n):
+    """Scenes of up to 12 surfaces are traced without sorting or culling, larger
+    ones through packets: both agree with the oracles ray by ray."""
+    from rayfactorcl_gb300 import generators
+    counts = (3, 3, 2, 2, n - 10)
+    sc = generators.mixed_scene(seed=11 + n, total_rays=4, counts=counts).scene
+    p = O.params(compat=0)
+    total = bad = 0
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        for e in range(0, n, 3):
+            got = t.trace_rays(e, 0, 8192)
+            e64 = O.trace_rays(sc, p, e, 0, 8192, f64=True)
+            e32 = O.trace_rays(sc, p, e, 0, 8192)
+            total += got.size
+            bad += int(np.count_nonzero((got != e64) & (got != e32)))
+    assert bad / total <= 2e-3, (bad, total)
+
+
 def test_mixed_beats_fp32_on_far_offsets(built_lib, oracle_lib):
     """Unit surfaces 1e4 from the origin, thin annuli, 89.9 degree frusta: the
     mixed kernel (re-centred, FP64 for ill-conditioned roots) agrees with the
