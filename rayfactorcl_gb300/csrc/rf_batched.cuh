@@ -28,7 +28,8 @@
 //      atomics whenever the (scene, emitter) row changes.
 // Skipping a surface whose bounding sphere no ray of the packet can reach does
 // not change any ray's nearest hit; only the arithmetic differs from the
-// exact kernel.
+// exact kernel.  Scenes of at most kBruteMax surfaces skip steps 1-3: every
+// thread tests its own rays against all surfaces (culling cannot pay there).
 #pragma once
 
 #include "rf_device.cuh"
@@ -100,8 +101,7 @@ __device__ __forceinline__ bool ray_may_hit(const Ray<float> &r, float idd, cons
     return fmaf(-bb * bb, idd, oc2) <= b.w;
 }
 
-// Bounds of a packet of rays (one per lane; invalid lanes excluded), the same
-// in every lane.
+// Bounds of a packet of 32 rays, the same in every lane.
 struct Packet {
     float ox, oy, oz, rho;  // origin ball
     float ax, ay, az;       // cone axis (unit)
@@ -300,7 +300,8 @@ __device__ __noinline__ float hit_f64(const HitRec &h, const Ray<float> &w, floa
 }
 
 // Full nearest-hit search for one ray with FP64 for every ill-conditioned
-// quadric (cold path: a packet deferred more tests than its queue holds).
+// quadric (cold path: the ray deferred more than one test, and a lane keeps
+// only one).
 __device__ __noinline__ int retrace_f64(int n, bool resident, const HitRec *stab, const HitRec *gtab,
                                         const Ray<float> &ray, float eps, bool sc)
 {
@@ -332,9 +333,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
     int cur_scene = -1, cur_emitter = -1;
     SceneInfo si{};
     int nref = 0;
-    // work counters (warp-uniform, counted by lane 0)
-    // work counters: per warp in shared memory (lane 0), folded per chunk into
-    // the block's 64-bit counters
+    // work counters: per warp in shared memory (lane 0; tests by type in the
+    // registers of lanes 0-5), folded per chunk into the block's 64-bit counters
     if (tid < 8) S.work[tid] = 0ull;
     if (lane < 8) S.wcount[warp][lane] = 0u;
     bool hist_on = false;
