@@ -190,6 +190,13 @@ rf_status rf_surface_areas(const rf_primitive *prims, int32_t n_prims, double *a
 rf_status rf_budgets_by_area(const rf_primitive *prims, int32_t n_prims, int64_t total_rays,
                              int64_t *rays_out);
 
+/* The same with the scene file's per-primitive <rayDensity value> honoured
+ * exactly: budgets proportional to density[i] * area[i] (density NULL: all 1).
+ * The reference reads that value (Scene.cpp:307-321) but folds it, truncated to
+ * an integer, into a truncated area proxy (Scene.cpp:362-387). */
+rf_status rf_budgets_by_density(const rf_primitive *prims, int32_t n_prims, const double *density,
+                                int64_t total_rays, int64_t *rays_out);
+
 /* Write F like main.cpp:236-249: one row per emitter, 8 significant digits,
  * every value followed by a comma. */
 rf_status rf_write_output_txt(const char *path, const double *F, int32_t n);

@@ -35,7 +35,7 @@ EXPORTS = ("rf_config_default", "rf_create", "rf_destroy", "rf_last_error", "rf_
            "rf_write_output_txt", "rf_trace_batch", "rf_converge_batch", "rf_check_F",
            "rf_autotune", "rf_last_refine_count", "rf_last_work_counts", "rf_measure_fp32_peak",
            "rf_trace_mixed_noalloc", "rf_get_launch_config", "rf_trace_range", "rf_set_tallies",
-           "rf_surface_areas", "rf_budgets_by_area", "rf_smooth_F")
+           "rf_surface_areas", "rf_budgets_by_area", "rf_budgets_by_density", "rf_smooth_F")
 
 
 class RfConfig(ctypes.Structure):
@@ -98,6 +98,7 @@ def load() -> ctypes.CDLL:
         "rf_surface_areas": (ctypes.c_int, [P, I32, P]),
         "rf_smooth_F": (ctypes.c_int, [P, P, P, I32, I32, P, ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_double)]),
         "rf_budgets_by_area": (ctypes.c_int, [P, I32, I64, P]),
+        "rf_budgets_by_density": (ctypes.c_int, [P, I32, P, I64, P]),
         "rf_last_refine_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
         "rf_last_work_counts": (ctypes.c_int, [P, P]),
         "rf_measure_fp32_peak": (ctypes.c_int, [I32, ctypes.POINTER(ctypes.c_double)]),

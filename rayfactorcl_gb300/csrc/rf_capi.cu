@@ -1004,11 +1004,22 @@ rf_status rf_surface_areas(const rf_primitive *prims, int32_t n, double *areas)
 
 rf_status rf_budgets_by_area(const rf_primitive *prims, int32_t n, int64_t total_rays, int64_t *rays_out)
 {
+    return rf_budgets_by_density(prims, n, nullptr, total_rays, rays_out);
+}
+
+rf_status rf_budgets_by_density(const rf_primitive *prims, int32_t n, const double *density, int64_t total_rays,
+                                int64_t *rays_out)
+{
     if (!prims || n <= 0 || !rays_out || total_rays < 0) return RF_ERR_INVALID_ARG;
     if (total_rays > (kMaxRaysPerEmitter / 2)) return RF_ERR_OVERFLOW;
     std::vector<double> a(n);
     rf_status s = rf_surface_areas(prims, n, a.data());
     if (s != RF_OK) return s;
+    if (density)
+        for (int i = 0; i < n; ++i) {
+            if (!(density[i] >= 0.0) || !std::isfinite(density[i])) return RF_ERR_INVALID_ARG;
+            a[i] *= density[i];
+        }
     double tot = 0.0;
     for (double v : a) tot += v;
     if (!(tot > 0.0)) return RF_ERR_BAD_SCENE;

@@ -47,6 +47,9 @@ class Scene:
     primitives: np.ndarray = field(default_factory=lambda: np.zeros(0, PRIM_DTYPE))
     bounding_volumes: np.ndarray = field(default_factory=lambda: np.zeros(0, BV_DTYPE))
     description: str = ""
+    # each primitive's <rayDensity value> from the file (Scene.cpp:307-321; 1 when
+    # absent), kept unrounded for area budgets; not part of the table bytes
+    density: np.ndarray | None = None
 
     @property
     def n(self) -> int:
@@ -318,6 +321,7 @@ class _Loader:
     def __init__(self):
         self.prims: list[np.void] = []
         self.bvs: list[np.void] = []
+        self.density: list[float] = []
 
     def load_geometry(self, geometry):
         """Scene.cpp:191-282."""
@@ -359,16 +363,17 @@ class _Loader:
                 rec["util2"] = bound_mod
             else:
                 continue  # type none is not stored (Scene.cpp:275)
-            self.init_primitive(el, rec)
+            self.density.append(self.init_primitive(el, rec))
             self.prims.append(rec)
 
     def init_primitive(self, el, rec):
         """Scene.cpp:296-390."""
         if not _has_child_node(el):
-            return  # the reference returns before touching the matrices
+            return 1.0  # the reference returns before touching the matrices
         xs, ys, zs, rd, _ = _init_transform(el, rec, True)
         rec["rayDensity"] = _ray_density(int(rec["type"]), rd, xs, ys, zs,
                                          F32(rec["util1"]), F32(rec["util2"]))
+        return float(rd)
 
     def load_bounding_volumes(self, geometry):
         """Scene.cpp:97-175."""
@@ -449,6 +454,7 @@ def parse_scene_xml(text: str) -> Scene:
     else:
         ld.load_geometry(geometry)
     sc.primitives = np.array(ld.prims, PRIM_DTYPE) if ld.prims else np.zeros(0, PRIM_DTYPE)
+    sc.density = np.array(ld.density, np.float64)
     sc.bounding_volumes = np.array(ld.bvs, BV_DTYPE) if ld.bvs else np.zeros(0, BV_DTYPE)
     return sc
 

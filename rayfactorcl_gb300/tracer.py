@@ -262,11 +262,17 @@ def surface_areas(scene: Scene) -> np.ndarray:
     return out
 
 
-def budgets_by_area(scene: Scene, total_rays: int) -> np.ndarray:
-    """total_rays spread over the emitters by area, multiples of four."""
+def budgets_by_area(scene: Scene, total_rays: int, use_density: bool = True) -> np.ndarray:
+    """total_rays spread over the emitters by area, multiples of four; weighted by
+    each primitive's <rayDensity> from the scene file when the scene has them."""
     prims = np.ascontiguousarray(scene.primitives, PRIM_DTYPE)
     out = np.zeros(prims.shape[0], np.int64)
-    check(_lib.load().rf_budgets_by_area(ptr(prims), prims.shape[0], int(total_rays), ptr(out)))
+    dens = getattr(scene, "density", None)
+    if use_density and dens is not None and len(dens) == prims.shape[0]:
+        d = np.ascontiguousarray(dens, np.float64)
+        check(_lib.load().rf_budgets_by_density(ptr(prims), prims.shape[0], ptr(d), int(total_rays), ptr(out)))
+    else:
+        check(_lib.load().rf_budgets_by_area(ptr(prims), prims.shape[0], int(total_rays), ptr(out)))
     return out
 
 

@@ -201,6 +201,21 @@ def test_surface_areas_and_area_budgets(built_lib):
         b = budgets_by_area(w.scene, 10**9)
         assert np.all(b % 4 == 0) and abs(int(b.sum()) - 10**9) < 4 * w.scene.n
         assert np.allclose(b / b.sum(), a / a.sum(), atol=1e-8)
+    # the file's <rayDensity> weights the area budgets exactly (the reference
+    # truncates it into its integer area proxy, Scene.cpp:362-387)
+    xml = """<project><settings><globalRayDensity value="1" /></settings><geometry>
+        <primitive type="disc"><rayDensity value="2.5" /><scale x="1" y="1" z="1" /></primitive>
+        <primitive type="disc"><scale x="1" y="1" z="1" /><translation x="0" y="0" z="1" /></primitive>
+        <primitive type="disc"><rayDensity value="0.5" /><scale x="2" y="2" z="1" /></primitive>
+        </geometry></project>"""
+    sc = parse_scene_xml(xml)
+    assert np.array_equal(sc.density, [2.5, 1.0, 0.5])
+    assert list(sc.primitives["rayDensity"]) == [6, 3, 0]  # (int)2.5*pi, pi, (int)0.5*4pi
+    b = budgets_by_area(sc, 10**8)
+    w = np.array([2.5 * math.pi, math.pi, 0.5 * 4 * math.pi])
+    assert np.allclose(b / b.sum(), w / w.sum(), atol=1e-7)
+    assert np.allclose(budgets_by_area(sc, 10**8, use_density=False) / 10**8,
+                       np.array([1, 1, 4]) / 6, atol=1e-7)
     # an ellipsoid: Knud Thomsen's formula (Scene.cpp:373-374) is within 1.061 %
     xml = """<project><settings><globalRayDensity value="1" /></settings><geometry>
         <primitive type="sphere"><scale x="1" y="2" z="3" /></primitive></geometry></project>"""
