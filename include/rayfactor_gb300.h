@@ -101,7 +101,9 @@ typedef struct rf_config {
     uint32_t scene_id;    /* folded into the stream counter outside RF_COMPAT_STREAMS       */
     int32_t tally_mode;   /* 0: autotuned / default; 1: shared-memory row histogram; 2: global atomics */
     int32_t table_mode;   /* 0: autotuned / default; 1: surfaces staged in shared memory; 2: read through L1 */
-    uint32_t reserved[5];
+    int32_t test_order;   /* 0: autotuned / default; 1: a thread's 4 or 8 rays tested together against
+                           * each surface; 2: one ray at a time against all surfaces (smaller code) */
+    uint32_t reserved[4];
 } rf_config;
 
 typedef struct rf_ctx rf_ctx;
@@ -254,8 +256,9 @@ rf_status rf_smooth_F(rf_ctx *ctx, const double *F, const double *areas, int32_t
  * timing runs of about 2^25 rays (spread over the emitters like the budgets of
  * the context's last trace, else evenly) of every combination of threads per block
  * (128, 256), rays per thread (4, 8), surface staging (shared-memory tiles or
- * reads through L1) and tallying (shared-memory row histogram or global
- * atomics); the choice is cached per scene shape in memory and, when cache_path
+ * reads through L1), tallying (shared-memory row histogram or global
+ * atomics) and test order (a thread's rays together per surface, or one ray
+ * at a time); the choice is cached per scene shape in memory and, when cache_path
  * is not NULL, appended to that file and read back by later processes.  Applies
  * the choice to the context.  A no-op for RF_PREC_MIXED (one launch shape).
  * Results of a trace do not depend on the launch shape. */
@@ -263,7 +266,7 @@ rf_status rf_autotune(rf_ctx *ctx, int32_t use_bv, const char *cache_path);
 
 /* (No counterpart in the reference.)  The launch shape the context uses now (after rf_autotune, or the defaults). */
 rf_status rf_get_launch_config(rf_ctx *ctx, int32_t *block, int32_t *rays_per_thread,
-                               int32_t *smem_hist, int32_t *smem_table);
+                               int32_t *smem_hist, int32_t *smem_table, int32_t *one_ray_at_a_time);
 
 /* (No counterpart in the reference.)  Counters of the last mixed-precision run: tests re-evaluated in FP64. */
 rf_status rf_last_refine_count(rf_ctx *ctx, uint64_t *refined_tests);

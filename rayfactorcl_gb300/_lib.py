@@ -44,7 +44,7 @@ class RfConfig(ctypes.Structure):
                 ("device", ctypes.c_int32), ("block_size", ctypes.c_int32),
                 ("rays_per_thread", ctypes.c_int32), ("scene_id", ctypes.c_uint32),
                 ("tally_mode", ctypes.c_int32), ("table_mode", ctypes.c_int32),
-                ("reserved", ctypes.c_uint32 * 5)]
+                ("test_order", ctypes.c_int32), ("reserved", ctypes.c_uint32 * 4)]
 
 
 class RfSceneDesc(ctypes.Structure):
@@ -92,7 +92,7 @@ def load() -> ctypes.CDLL:
         "rf_check_F": (ctypes.c_int, [P, P, P, I32, ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(ctypes.c_double)]),
         "rf_autotune": (ctypes.c_int, [P, I32, ctypes.c_char_p]),
-        "rf_get_launch_config": (ctypes.c_int, [P, P, P, P, P]),
+        "rf_get_launch_config": (ctypes.c_int, [P, P, P, P, P, P]),
         "rf_trace_range": (ctypes.c_int, [P, P, P, I32, I32]),
         "rf_set_tallies": (ctypes.c_int, [P, P, P]),
         "rf_surface_areas": (ctypes.c_int, [P, I32, P]),

@@ -111,7 +111,7 @@ struct rf_ctx {
     bool timed = false;
 
     // launch choices (0 / -1 = default); set by rf_config or rf_autotune
-    int block = 0, gpt = 0, hist = -1, stage = -1;
+    int block = 0, gpt = 0, hist = -1, stage = -1, order = -1;  // order 1: one ray at a time
 
     // batched mixed-precision path: scenes concatenated, re-centred in FP64
     DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters;
@@ -250,6 +250,7 @@ Plan make_plan(rf_ctx *c, bool bv, bool rec)
     pl.hist = !rec && (c->hist >= 0 ? c->hist == 1 : true) && c->n <= kHistMax;
     pl.stage = !bv && (rec || (c->stage >= 0 ? c->stage == 1 : true));
     pl.lc.stage = pl.stage;
+    pl.lc.serial = !bv && !rec && c->order == 1;
     const int tab = pl.stage ? std::min(c->n, kTile) : 0;
     pl.lc.smem = (size_t)tab * sizeof(HitRec) + (pl.hist ? (size_t)c->n * 4 : 0);
     return pl;
@@ -607,6 +608,7 @@ rf_status rf_create(rf_ctx **out, const rf_config *cfg)
     ctx->device = c.device;
     if (c.tally_mode) ctx->hist = c.tally_mode == 1 ? 1 : 0;
     if (c.table_mode) ctx->stage = c.table_mode == 1 ? 1 : 0;
+    if (c.test_order) ctx->order = c.test_order == 2 ? 1 : 0;
     if (cudaSetDevice(c.device) != cudaSuccess ||
         cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1304,15 +1306,16 @@ rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_sc
 // Autotuner of the single-scene kernels: times every launch shape on a short
 // trace of the current scene and keeps the fastest.  Knobs: threads per block
 // (128 / 256), Philox draws per thread (1 / 2, i.e. 4 or 8 rays in registers),
-// surface staging (shared-memory tiles / reads through L1) and tallying (row
-// histogram in shared memory / warp-aggregated global atomics).  Results are
+// surface staging (shared-memory tiles / reads through L1), tallying (row
+// histogram in shared memory / warp-aggregated global atomics) and test order
+// (a thread's rays together per surface / one ray at a time).  Results are
 // cached per scene shape (precision, kernel, surface count and type mix, SM
-// count) in memory and, optionally, in a text file of "key|block gpt hist stage"
-// lines.  The mixed-precision kernel has one launch shape (a persistent grid of
+// count) in memory and, optionally, in a text file of
+// "key|block gpt hist stage order" lines.  The mixed-precision kernel has one launch shape (a persistent grid of
 // 1024-thread blocks) and needs no tuning.
 namespace {
 struct TuneChoice {
-    int block, gpt, hist, stage;
+    int block, gpt, hist, stage, order;
 };
 std::mutex g_tune_mu;
 std::map<std::string, TuneChoice> g_tune_cache;
@@ -1322,7 +1325,7 @@ std::string tune_key(const rf_ctx *c, int use_bv)
     int types[6] = {0, 0, 0, 0, 0, 0};
     for (const rf_primitive &p : c->prims) ++types[p.type];
     std::ostringstream k;
-    k << "v1 prec=" << c->cfg.precision << " bv=" << use_bv << " n=" << c->n << " nbv=" << c->nbv << " t=";
+    k << "v2 prec=" << c->cfg.precision << " bv=" << use_bv << " n=" << c->n << " nbv=" << c->nbv << " t=";
     for (int i = 0; i < 6; ++i) k << types[i] << (i < 5 ? "," : "");
     k << " sm=" << c->sms;
     return k.str();
@@ -1338,7 +1341,7 @@ bool tune_lookup_file(const char *path, const std::string &key, TuneChoice &out)
         if (bar == std::string::npos || line.compare(0, bar, key) != 0 || bar != key.size()) continue;
         std::istringstream v(line.substr(bar + 1));
         TuneChoice t{};
-        if (v >> t.block >> t.gpt >> t.hist >> t.stage) {
+        if (v >> t.block >> t.gpt >> t.hist >> t.stage >> t.order) {
             out = t;
             found = true;  // the last entry wins
         }
@@ -1352,6 +1355,7 @@ void tune_apply(rf_ctx *c, const TuneChoice &t)
     c->gpt = t.gpt;
     c->hist = t.hist;
     c->stage = t.stage;
+    c->order = t.order;
 }
 }  // namespace
 
@@ -1392,15 +1396,17 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
     const bool bv = use_bv != 0;
     const bool wide = !bv && c->cfg.precision != RF_PREC_FP64;
     double best_ms = 1e300;
-    const TuneChoice saved{c->block, c->gpt, c->hist, c->stage};
+    const TuneChoice saved{c->block, c->gpt, c->hist, c->stage, c->order};
     for (int block : {128, 256})
         for (int gpt : {1, 2}) {
             if (gpt == 2 && !wide) continue;
             for (int hist : {1, 0}) {
                 if (hist && c->n > kHistMax) continue;
-                for (int stage : {1, 0}) {
+                for (int stage : {1, 0})
+                for (int order : {0, 1}) {
                     if (bv && stage == 0) continue;  // the bounding-surface kernel reads through L1 anyway
-                    tune_apply(c, TuneChoice{block, gpt, hist, stage});
+                    if (bv && order == 1) continue;  // and tests one ray at a time anyway
+                    tune_apply(c, TuneChoice{block, gpt, hist, stage, order});
                     double ms_min = 1e300;
                     for (int rep = 0; rep < 3; ++rep) {
                         if ((s = rf_trace_async(c, rays.data(), use_bv)) != RF_OK) {
@@ -1416,7 +1422,7 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
                     }
                     if (ms_min < best_ms) {
                         best_ms = ms_min;
-                        best = TuneChoice{block, gpt, hist, stage};
+                        best = TuneChoice{block, gpt, hist, stage, order};
                     }
                 }
             }
@@ -1429,19 +1435,21 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
     }
     if (cache_path) {
         std::ofstream f(cache_path, std::ios::app);
-        if (f) f << key << "|" << best.block << " " << best.gpt << " " << best.hist << " " << best.stage << "\n";
+        if (f) f << key << "|" << best.block << " " << best.gpt << " " << best.hist << " " << best.stage << " "
+                 << best.order << "\n";
     }
     return RF_OK;
 }
 
 rf_status rf_get_launch_config(rf_ctx *c, int32_t *block, int32_t *rays_per_thread, int32_t *smem_hist,
-                               int32_t *smem_table)
+                               int32_t *smem_table, int32_t *one_ray_at_a_time)
 {
     if (!c) return RF_ERR_INVALID_ARG;
     if (block) *block = c->block > 0 ? c->block : (c->cfg.block_size > 0 ? c->cfg.block_size : kBlock);
     if (rays_per_thread) *rays_per_thread = 4 * (c->gpt > 0 ? c->gpt : (c->cfg.rays_per_thread == 8 ? 2 : 1));
     if (smem_hist) *smem_hist = c->hist >= 0 ? c->hist : 1;
     if (smem_table) *smem_table = c->stage >= 0 ? c->stage : 1;
+    if (one_ray_at_a_time) *one_ray_at_a_time = c->order == 1 ? 1 : 0;
     return RF_OK;
 }
 

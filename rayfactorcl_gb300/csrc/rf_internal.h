@@ -82,6 +82,7 @@ struct LaunchCfg {
     bool bv = false;    // runBVGPU semantics
     bool rec = false;   // write per-ray hit indices instead of tallying
     bool stage = true;  // surfaces staged in shared memory (else read through L1)
+    bool serial = false; // one ray at a time against all surfaces (else a thread's rays together)
 };
 
 // Implemented once per arithmetic policy (rf_kern_exact.cu, rf_kern_fast.cu).

@@ -80,7 +80,7 @@ __device__ __forceinline__ int trace_bv(const TraceParams &p, const Ray<typename
     return obj;
 }
 
-template <class M, int GPT, bool BV, bool REC, bool STAGE>
+template <class M, int GPT, bool BV, bool REC, bool STAGE, bool SERIAL>
 __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
 {
     using T = typename M::T;
@@ -168,6 +168,48 @@ __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
         if (BV) {
 #pragma unroll
             for (int k = 0; k < R; ++k) bi[k] = trace_bv<M>(p, ray[k], eps, sc);
+        } else if (SERIAL) {
+            // One ray at a time against the table: a single copy of each surface
+            // test in the instruction stream (the 4- or 8-ray unrolled tests with
+            // the IEEE sequences of the exact mapping strain the instruction cache)
+            // and half the registers (the rays wait in local memory).  Faster on
+            // small scenes; the autotuner decides.
+            T tb[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) { tb[k] = M::inf(); bi[k] = -1; }
+            const int step = stage ? kTile : n;
+            for (int t0 = 0; t0 < n; t0 += step) {
+                const int cnt = min(step, n - t0);
+                if (tiled) {
+                    __syncthreads();
+                    const float4 *src = reinterpret_cast<const float4 *>(p.tab + t0);
+                    float4 *dst = reinterpret_cast<float4 *>(s_tab);
+                    for (int i = tid; i < 4 * cnt; i += blockDim.x) dst[i] = __ldg(src + i);
+                    __syncthreads();
+                }
+#pragma unroll 1
+                for (int k = 0; k < R; ++k) {
+                    const Ray<T> rk = ray[k];
+                    T tbk = tb[k];
+                    int bik = bi[k];
+                    for (int jj = 0; jj < cnt; ++jj) {
+                        const HitRec h = stage ? s_tab[jj] : load_rec(p.tab, t0 + jj);
+                        T t;
+                        switch (__float_as_int(h.aux.x)) {  // warp-uniform
+                        case RF_DISC: t = disc_hit<M>(h, rk, eps); break;
+                        case RF_ANNULUS: t = annulus_hit<M>(h, rk, eps); break;
+                        case RF_RECTANGLE: t = rectangle_hit<M>(h, rk, eps); break;
+                        case RF_CYLINDER: t = cylinder_hit<M>(h, rk, eps); break;
+                        case RF_FRUSTUM: t = frustum_hit<M>(h, rk, eps); break;
+                        case RF_SPHERE: t = sphere_hit<M>(h, rk, eps, sc); break;
+                        default: t = M::inf(); break;  // validated away on the host
+                        }
+                        if (t < tbk) { tbk = t; bik = t0 + jj; }
+                    }
+                    tb[k] = tbk;
+                    bi[k] = bik;
+                }
+            }
         } else {
             T tb[R];
 #pragma unroll
@@ -223,10 +265,10 @@ __global__ void __launch_bounds__(kBlock) trace_kernel(const TraceParams p)
     if (hist && sg.emitter >= 0) flush(sg.emitter);
 }
 
-template <class M, int GPT, bool BV, bool REC, bool STAGE>
+template <class M, int GPT, bool BV, bool REC, bool STAGE, bool SERIAL>
 static cudaError_t launch_one(const LaunchCfg &cfg, const TraceParams &p, cudaStream_t st)
 {
-    auto k = trace_kernel<M, GPT, BV, REC, STAGE>;
+    auto k = trace_kernel<M, GPT, BV, REC, STAGE, SERIAL>;
     if (cfg.smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
         if (e != cudaSuccess) return e;
@@ -235,11 +277,11 @@ static cudaError_t launch_one(const LaunchCfg &cfg, const TraceParams &p, cudaSt
     return cudaGetLastError();
 }
 
-template <class M, int GPT, bool BV, bool REC, bool STAGE>
+template <class M, int GPT, bool BV, bool REC, bool STAGE, bool SERIAL>
 static int occupancy_one(const LaunchCfg &cfg)
 {
     int nb = 0;
-    auto k = trace_kernel<M, GPT, BV, REC, STAGE>;
+    auto k = trace_kernel<M, GPT, BV, REC, STAGE, SERIAL>;
     if (cfg.smem > 48 * 1024)
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, cfg.block, cfg.smem) != cudaSuccess)
@@ -247,19 +289,24 @@ static int occupancy_one(const LaunchCfg &cfg)
     return nb;
 }
 
+#define RF_DISPATCH_S(FN, S, ...)                                                   \
+    do {                                                                            \
+        if (cfg.gpt == 2) {                                                         \
+            if (cfg.stage) return FN<M, 2, false, false, true, S>(__VA_ARGS__);     \
+            return FN<M, 2, false, false, false, S>(__VA_ARGS__);                   \
+        }                                                                           \
+        if (cfg.stage) return FN<M, 1, false, false, true, S>(__VA_ARGS__);         \
+        return FN<M, 1, false, false, false, S>(__VA_ARGS__);                       \
+    } while (0)
 #define RF_DISPATCH(FN, ...)                                                        \
     do {                                                                            \
         if (cfg.rec) {                                                              \
-            if (cfg.bv) return FN<M, 1, true, true, false>(__VA_ARGS__);            \
-            return FN<M, 1, false, true, true>(__VA_ARGS__);                        \
+            if (cfg.bv) return FN<M, 1, true, true, false, false>(__VA_ARGS__);     \
+            return FN<M, 1, false, true, true, false>(__VA_ARGS__);                 \
         }                                                                           \
-        if (cfg.bv) return FN<M, 1, true, false, false>(__VA_ARGS__);               \
-        if (cfg.gpt == 2) {                                                         \
-            if (cfg.stage) return FN<M, 2, false, false, true>(__VA_ARGS__);        \
-            return FN<M, 2, false, false, false>(__VA_ARGS__);                      \
-        }                                                                           \
-        if (cfg.stage) return FN<M, 1, false, false, true>(__VA_ARGS__);            \
-        return FN<M, 1, false, false, false>(__VA_ARGS__);                          \
+        if (cfg.bv) return FN<M, 1, true, false, false, false>(__VA_ARGS__);        \
+        if (cfg.serial) RF_DISPATCH_S(FN, true, __VA_ARGS__);                       \
+        RF_DISPATCH_S(FN, false, __VA_ARGS__);                                      \
     } while (0)
 
 template <class M>
@@ -275,5 +322,6 @@ int trace_blocks_per_sm(const LaunchCfg &cfg)
 }
 
 #undef RF_DISPATCH
+#undef RF_DISPATCH_S
 
 }  // namespace rf

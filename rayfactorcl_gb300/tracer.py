@@ -28,7 +28,7 @@ class Tracer:
 
     def __init__(self, precision: int = PREC_EXACT, compat: int = 0, key1: int = REF_KEY1,
                  eps: float = 1e-3, device: int = 0, block_size: int = 0, rays_per_thread: int = 0,
-                 scene_id: int = 0, tally_mode: int = 0, table_mode: int = 0):
+                 scene_id: int = 0, tally_mode: int = 0, table_mode: int = 0, test_order: int = 0):
         L = _lib.load()
         cfg = _lib.RfConfig()
         L.rf_config_default(ctypes.byref(cfg))
@@ -42,6 +42,7 @@ class Tracer:
         cfg.scene_id = scene_id & 0xFFFFFFFF
         cfg.tally_mode = tally_mode
         cfg.table_mode = table_mode
+        cfg.test_order = test_order
         h = ctypes.c_void_p()
         check(L.rf_create(ctypes.byref(h), ctypes.byref(cfg)))
         self._h = h
@@ -158,10 +159,10 @@ class Tracer:
         return self.launch_config()
 
     def launch_config(self) -> dict:
-        v = [ctypes.c_int32() for _ in range(4)]
+        v = [ctypes.c_int32() for _ in range(5)]
         self._check(self._L.rf_get_launch_config(self._h, *[ctypes.byref(x) for x in v]))
         return {"block": v[0].value, "rays_per_thread": v[1].value, "smem_hist": v[2].value,
-                "smem_table": v[3].value}
+                "smem_table": v[3].value, "one_ray_at_a_time": v[4].value}
 
     def refined_count(self) -> int:
         """Quadric tests re-evaluated in FP64 by the last mixed-precision run."""

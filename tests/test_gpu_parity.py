@@ -61,10 +61,10 @@ def test_exact_tallies(built_lib, oracle_lib, name, compat):
         rays[1] = 4 * 257 + 3
     p = O.params(compat=compat, use_bv=use_bv)
     exp = O.tally(sc, p, rays)
-    for gpt in (4, 8):
-        with _tracer(sc, precision=PREC_EXACT, compat=compat, rays_per_thread=gpt) as t:
+    for gpt, order in ((4, 1), (8, 1), (4, 2), (8, 2)):  # rays together / one ray at a time
+        with _tracer(sc, precision=PREC_EXACT, compat=compat, rays_per_thread=gpt, test_order=order) as t:
             hits, F = t.trace(rays, use_bv=use_bv)
-        assert np.array_equal(hits, exp), (name, gpt, np.argwhere(hits != exp)[:5])
+        assert np.array_equal(hits, exp), (name, gpt, order, np.argwhere(hits != exp)[:5])
         assert np.isnan(F[0]).all()
         nz = rays > 0
         assert np.allclose(F[nz], exp[nz] / rays[nz, None], rtol=0, atol=0)
