@@ -338,6 +338,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
     if (tid < 8) S.work[tid] = 0ull;
     if (lane < 8) S.wcount[warp][lane] = 0u;
     bool hist_on = false;
+    int row_chunks = 0;   // chunks tallied into the shared-memory row since its last flush
     uint32_t tcount = 0;  // lane t < 6: lane-tests of surfaces of type t by this warp (this chunk)
 
     auto flush = [&]() {
@@ -363,8 +364,13 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
         const int s = find_segment(p.seg, nseg, c);
         const Segment sg = p.seg[s];
 
+        if (!REC && hist_on && ++row_chunks >= 32768) {  // keep the 32-bit bins far from overflow
+            flush();                                     // (at most 32768 hits per bin per chunk)
+            row_chunks = 0;
+        }
         if (sg.scene != cur_scene || sg.emitter != cur_emitter) {
             if (!REC) flush();
+            row_chunks = 0;
             if (sg.scene != cur_scene) {
                 si = p.scenes[sg.scene];
                 eps = si.eps;
