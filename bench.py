@@ -49,7 +49,9 @@ def algorithmic_ops(scene, rays) -> float:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 25 ms (the headline's
+    timed region is a few tens of ms); entering waits for the first sample so that
+    the region is covered."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -65,10 +67,13 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "25"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.perf_counter()
+            while not self.rows and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.005)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -81,6 +86,10 @@ class ClockSampler:
 
     def __exit__(self, *exc):
         if self.proc is not None:
+            n = len(self.rows)  # one more sample, taken at the end of the region
+            t0 = time.perf_counter()
+            while len(self.rows) == n and time.perf_counter() - t0 < 1.0 and self.proc.poll() is None:
+                time.sleep(0.005)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
