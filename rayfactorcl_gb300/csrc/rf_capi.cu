@@ -755,6 +755,8 @@ rf_status rf_trace_range(rf_ctx *c, const int64_t *first_ray, const int64_t *cou
     std::vector<int64_t> ends(c->n);
     for (int e = 0; e < c->n; ++e) {
         if (first_ray[e] < 0 || count[e] < 0) return fail(c, RF_ERR_INVALID_ARG, "negative ray range (emitter %d)", e);
+        if (first_ray[e] > kMaxRaysPerEmitter || count[e] > kMaxRaysPerEmitter)
+            return fail(c, RF_ERR_OVERFLOW, "ray range of emitter %d beyond 2^46", e);
         ends[e] = first_ray[e] + count[e];
     }
     if ((s = check_budgets(c, ends.data(), c->n)) != RF_OK) return s;
