@@ -103,6 +103,20 @@ def test_mixed_brute_force_boundary(built_lib, oracle_lib, n):
     assert bad / total <= 2e-3, (bad, total)
 
 
+def test_mixed_per_ray_ragged_ranges(built_lib, oracle_lib):
+    """Ray ranges that start and end inside a Philox draw (4 rays) and inside a
+    32768-ray chunk: every ray keeps its stream position."""
+    sc = golden_scene("gen_mixed64")
+    p = O.params(compat=0)
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        for e, first, n in ((3, 5, 3001), (40, 32766, 7), (63, 65537, 40003)):
+            got = t.trace_rays(e, first, n)
+            e64 = O.trace_rays(sc, p, e, first, first + n, f64=True)
+            e32 = O.trace_rays(sc, p, e, first, first + n)
+            bad = int(np.count_nonzero((got != e64) & (got != e32)))
+            assert bad <= max(2, 2e-3 * n), (e, first, n, bad)
+
+
 def test_mixed_beats_fp32_on_far_offsets(built_lib, oracle_lib):
     """Unit surfaces 1e4 from the origin, thin annuli, 89.9 degree frusta: the
     mixed kernel (re-centred, FP64 for ill-conditioned roots) agrees with the
