@@ -31,27 +31,29 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        so = _build.build_oracle()
-        L = ctypes.CDLL(str(so))
-        P = ctypes.c_void_p
-        L.rfo_philox4x32_10.argtypes = [P, P, P]
-        L.rfo_sincosf_array.argtypes = [P, ctypes.c_int64, P, P]
-        L.rfo_stream_uniforms.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.c_int64, P]
-        L.rfo_emit_ray.argtypes = [P, ctypes.c_int32, ctypes.POINTER(Params), ctypes.c_int64, P, P]
-        for name in ("rfo_trace_rays", "rfo_trace_rays_f64"):
-            getattr(L, name).argtypes = [P, ctypes.c_int32, P, ctypes.c_int32, ctypes.POINTER(Params),
-                                         ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, P,
-                                         ctypes.c_int32]
-            getattr(L, name).restype = ctypes.c_int
-        for name in ("rfo_tally", "rfo_tally_f64"):
-            getattr(L, name).argtypes = [P, ctypes.c_int32, P, ctypes.c_int32, ctypes.POINTER(Params),
-                                         ctypes.c_int32, ctypes.c_int64, P, ctypes.c_int32]
-            getattr(L, name).restype = ctypes.c_int
-        L.rfo_ref_nthreads.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
-        L.rfo_ref_nthreads.restype = ctypes.c_int64
-        L.rfo_max_threads.restype = ctypes.c_int32
-        _lib = L
+        _lib = _bind(ctypes.CDLL(str(_build.build_oracle())))
     return _lib
+
+
+def _bind(L):
+    P = ctypes.c_void_p
+    L.rfo_philox4x32_10.argtypes = [P, P, P]
+    L.rfo_sincosf_array.argtypes = [P, ctypes.c_int64, P, P]
+    L.rfo_stream_uniforms.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.c_int64, P]
+    L.rfo_emit_ray.argtypes = [P, ctypes.c_int32, ctypes.POINTER(Params), ctypes.c_int64, P, P]
+    for name in ("rfo_trace_rays", "rfo_trace_rays_f64"):
+        getattr(L, name).argtypes = [P, ctypes.c_int32, P, ctypes.c_int32, ctypes.POINTER(Params),
+                                     ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, P,
+                                     ctypes.c_int32]
+        getattr(L, name).restype = ctypes.c_int
+    for name in ("rfo_tally", "rfo_tally_f64"):
+        getattr(L, name).argtypes = [P, ctypes.c_int32, P, ctypes.c_int32, ctypes.POINTER(Params),
+                                     ctypes.c_int32, ctypes.c_int64, P, ctypes.c_int32]
+        getattr(L, name).restype = ctypes.c_int
+    L.rfo_ref_nthreads.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+    L.rfo_ref_nthreads.restype = ctypes.c_int64
+    L.rfo_max_threads.restype = ctypes.c_int32
+    return L
 
 
 def _ptr(a: np.ndarray):
@@ -99,10 +101,11 @@ def _tables(scene):
 
 
 def trace_rays(scene, p: Params, emitter: int, ray_begin: int, ray_end: int,
-               f64: bool = False, threads: int = 0) -> np.ndarray:
+               f64: bool = False, threads: int = 0, lib_=None) -> np.ndarray:
     prims, bvs = _tables(scene)
     out = np.full(ray_end - ray_begin, -7, np.int32)
-    fn = lib().rfo_trace_rays_f64 if f64 else lib().rfo_trace_rays
+    L = lib_ if lib_ is not None else lib()
+    fn = L.rfo_trace_rays_f64 if f64 else L.rfo_trace_rays
     rc = fn(_ptr(prims), prims.shape[0], _ptr(bvs), bvs.shape[0], ctypes.byref(p), emitter,
             ray_begin, ray_end, _ptr(out), threads)
     if rc != 0:
@@ -135,6 +138,20 @@ def ref_nthreads(ray_density: int, n_samples: int, wg: int = 128) -> int:
 
 def max_threads() -> int:
     return int(lib().rfo_max_threads())
+
+
+def load_variant(path) -> ctypes.CDLL:
+    """Bind an oracle build made by build.build_oracle_variant (tests only)."""
+    return _bind(ctypes.CDLL(str(path)))
+
+
+# Per-ray fixture written by the reference's own kernel (tests/golden/make_golden.py)
+REF_WINDOWS = ((0, 8), (1048573, 1048581))
+
+
+def window_rays(windows=REF_WINDOWS):
+    """(ray_begin, ray_end) of each work-item window of the per-ray fixture."""
+    return [(4 * g0, 4 * g1) for g0, g1 in windows]
 
 
 GOLDEN = Path(__file__).resolve().parent.parent / "tests" / "golden"

@@ -53,8 +53,9 @@ void rfo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 /* three-part Cody-Waite split of pi/2 (W. Cody, W. Waite, "Software Manual  */
 /* for the Elementary Functions", 1980), then the Taylor series of sin       */
 /* (to r^9) and cos (to r^10) on |r| <= pi/4 in Horner form with fmaf.       */
-/* Truncation error < 3e-9 relative; the CUDA library evaluates the same     */
-/* sequence, so both produce identical bits.                                 */
+/* Truncation error < 3e-9 relative.  This project's CUDA code evaluates the */
+/* same sequence in its own own_sincosf (csrc/rf_device.cuh), so both give   */
+/* identical bits; no vendor math library is involved on either side.       */
 /* ------------------------------------------------------------------------ */
 static const float RFO_2_OVER_PI = 0x1.45f306p-1f;   /* float(2/pi)               */
 static const float RFO_PIO2_1 = 0x1.921fb6p+0f;      /* float(pi/2)               */
@@ -343,7 +344,13 @@ static rayf emit(const rfo_prim *e, const float r[4])
     case RFO_DISC: /* RFG:298-321 */
         rfo_sincosf(r[0] * RFO_2PI_F, &sn, &cs);
         t = sqrtf(r[1]);
+#ifdef RFO_PLANTED_DISC_SWAP
+        /* a deliberate convention slip, compiled only by the test that shows the
+         * per-ray pin against the reference kernel catches it */
+        p.x = t * cs; p.y = t * sn; p.z = 0.f;
+#else
         p.x = t * sn; p.y = t * cs; p.z = 0.f;
+#endif
         ray.s = transform_point(e->m, p);
         o = os_ray_direction(r);
         n = transform_normal(e->invm, zn);

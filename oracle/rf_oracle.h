@@ -9,10 +9,12 @@
  * Parity pins: the Philox stream is pinned against the reference's own
  * Random123/philox.h compiled on the host (tests/golden/philox_kat.json), the
  * scene tables against the reference's Scene.cpp/affine code compiled on the
- * host (tests/golden/scenes/), and the geometry against closed-form view
- * factors.  The OpenCL C kernel itself cannot be compiled on a host without an
- * OpenCL runtime, so the per-ray arithmetic is pinned through this restatement
- * and its fixed IEEE op mapping:
+ * host (tests/golden/scenes/), and every ray's first hit against the
+ * reference's own kernel source RayFactorGPU.cl, compiled as host C++ through
+ * oracle/ref_tools/cl_compat.h and run work-item by work-item
+ * (tests/golden/ref_kernel_rays.npz; equal on all 18 fixture scenes for runGPU
+ * and runBVGPU under RFO_COMPAT_*, all set).  OpenCL leaves the builtins'
+ * results implementation-defined, so both sides use one fixed IEEE op mapping:
  *   mad(a,b,c)      -> fmaf(a,b,c)
  *   native_sqrt(x)  -> sqrtf(x)             (correctly rounded)
  *   native_recip(x) -> 1.0f / x             (correctly rounded)

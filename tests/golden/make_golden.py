@@ -9,8 +9,14 @@ Run from the repository root:  python tests/golden/make_golden.py
   reference's Scene.cpp + TinyXML-2 + affine code (oracle/_ref/ref_scene_dump)
   for every sample geometry of the reference and for the seeded workload
   scenes whose XML is committed beside them as ``scenes/gen_<name>.xml``.
+* ``ref_kernel_rays.npz`` -- per-ray first-hit surfaces (-1 = none) written by
+  the reference's own kernel source, RayFactorCL/RayFactorGPU.cl compiled on the
+  host (oracle/_ref/librf_refkernel.so): runGPU on every scene above and
+  runBVGPU on those with bounding surfaces, for work-items REF_WINDOWS of every
+  emitter.  Key ``<scene>:<kernel>``, value int16 [n_emitters, 4 x work-items].
 
-Needs the reference checkout (RF_REFERENCE_DIR, default /root/reference).
+Needs the reference checkout (RF_REFERENCE_DIR, else ``reference`` beside the
+repository).
 """
 from __future__ import annotations
 
@@ -87,12 +93,62 @@ def make_scenes():
     return names
 
 
+# work-item (global id) windows of the per-ray fixture: the first ids, and a
+# window across 2^20 at an odd offset
+from oracle.oracle import REF_WINDOWS  # noqa: E402
+
+
+def ref_kernel_rays(lib, scene, use_bv: int, windows=REF_WINDOWS) -> np.ndarray:
+    """Per-ray hits of the compiled reference kernel for every emitter."""
+    import ctypes
+    prims = np.ascontiguousarray(scene.primitives)
+    bvs = np.ascontiguousarray(scene.bounding_volumes)
+    rows = []
+    for e in range(scene.n):
+        parts = []
+        for g0, g1 in windows:
+            out = np.full(4 * (g1 - g0), -7, np.int32)
+            rc = lib.rfr_trace_rays(prims.ctypes.data, prims.shape[0],
+                                    bvs.ctypes.data if bvs.shape[0] else None, bvs.shape[0],
+                                    use_bv, e, g0, g1, out.ctypes.data)
+            if rc != 0:
+                raise RuntimeError(f"reference kernel failed ({rc})")
+            parts.append(out)
+        rows.append(np.concatenate(parts))
+    return np.stack(rows)
+
+
+def load_ref_kernel():
+    import ctypes
+    lib = ctypes.CDLL(str(obuild.REF_KERNEL))
+    P = ctypes.c_void_p
+    lib.rfr_trace_rays.argtypes = [P, ctypes.c_int32, P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                   ctypes.c_int64, ctypes.c_int64, P]
+    lib.rfr_trace_rays.restype = ctypes.c_int
+    return lib
+
+
+def make_ref_rays(names):
+    from rayfactorcl_gb300.scene import Scene
+    lib = load_ref_kernel()
+    data = {}
+    for name in names:
+        sc = Scene.from_bytes((SCENES / f"{name}.bin").read_bytes())
+        kernels = ["runGPU"] + (["runBVGPU"] if sc.bounding_volumes.shape[0] else [])
+        for k in kernels:
+            data[f"{name}:{k}"] = ref_kernel_rays(lib, sc, int(k == "runBVGPU")).astype(np.int16)
+    np.savez_compressed(HERE / "ref_kernel_rays.npz", **data)
+    return sum(v.size for v in data.values())
+
+
 def main():
     if not obuild.build_ref():
         print("reference checkout not found; nothing regenerated")
         return 1
     print("philox vectors:", make_kat())
-    print("scenes:", ", ".join(make_scenes()))
+    names = make_scenes()
+    print("scenes:", ", ".join(names))
+    print("reference-kernel rays:", make_ref_rays(names))
     return 0
 
 

@@ -46,6 +46,24 @@ def test_exact_per_ray_hits(built_lib, oracle_lib, name, compat):
                 assert bad.size == 0, (name, e, first, bad[:8], got[bad[:8]], exp[bad[:8]])
 
 
+def test_exact_per_ray_equals_reference_kernel(built_lib):
+    """The CUDA kernels against the reference's own kernel source directly: every
+    ray of tests/golden/ref_kernel_rays.npz (RayFactorGPU.cl's runGPU and runBVGPU
+    compiled as host C++, two windows of work-items of every emitter of all 18
+    fixture scenes, RF_COMPAT_ALL) has the same first hit in the EXACT kernel."""
+    data = np.load(O.GOLDEN / "ref_kernel_rays.npz")
+    assert len(data.files) >= 21
+    for key in data.files:
+        name, kernel = key.split(":")
+        sc = golden_scene(name)
+        use_bv = kernel == "runBVGPU"
+        want = data[key]
+        with _tracer(sc, precision=PREC_EXACT, compat=_lib.COMPAT_ALL) as t:
+            for e in range(sc.n):
+                got = np.concatenate([t.trace_rays(e, a, b - a, use_bv=use_bv) for a, b in O.window_rays()])
+                assert np.array_equal(got, want[e]), (key, e, np.nonzero(got != want[e])[0][:8])
+
+
 @pytest.mark.parametrize("compat", COMPATS)
 @pytest.mark.parametrize("name", ["gen_enclosure3", "gen_mixed64", "input-C52-BV", "input-furnace",
                                   "gen_furnace", "input-C122", "gen_sweep0"])

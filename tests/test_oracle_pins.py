@@ -133,3 +133,83 @@ def test_ref_launch_size_ties_round_down(oracle_lib):
 def test_generated_scene_matches_reference_loader():
     for name in ["gen_enclosure3", "gen_mixed64", "gen_furnace", "gen_precision_stress"]:
         assert gen_scene(name).to_bytes() == golden_scene(name).to_bytes()
+
+
+# --- per-ray pin to the reference's own kernel source ------------------------
+# tests/golden/ref_kernel_rays.npz holds the first hit of every ray that the
+# reference's RayFactorGPU.cl (runGPU :481-527, runBVGPU :530-626), compiled as
+# host C++ by oracle/build.py, traced for two windows of work-items of every
+# emitter of all 18 fixture scenes.  Streams, sphere discriminant and stale
+# bounding-surface index are the reference's (RF_COMPAT_ALL).
+
+def _ref_rays():
+    data = np.load(GOLDEN / "ref_kernel_rays.npz")
+    return {k: data[k] for k in data.files}
+
+
+def _oracle_rows(sc, use_bv, lib_=None):
+    rows = []
+    for e in range(sc.n):
+        rows.append(np.concatenate([O.trace_rays(sc, O.params(use_bv=use_bv), e, a, b, lib_=lib_)
+                                    for a, b in O.window_rays()]))
+    return np.stack(rows)
+
+
+def test_reference_kernel_fixture_covers_every_scene():
+    from helpers import SAMPLE_NAMES, GEN_NAMES
+    ref = _ref_rays()
+    for name in SAMPLE_NAMES + GEN_NAMES:
+        assert f"{name}:runGPU" in ref
+        if golden_scene(name).bounding_volumes.shape[0]:
+            assert f"{name}:runBVGPU" in ref
+    hit = np.concatenate([v.ravel() for v in ref.values()])
+    assert hit.size > 100000 and 0.3 < float(np.mean(hit >= 0)) < 0.95
+
+
+def test_oracle_equals_reference_kernel_per_ray(oracle_lib):
+    """Every ray of the fixture: the oracle's first hit equals the reference kernel's."""
+    for key, want in _ref_rays().items():
+        name, kernel = key.split(":")
+        got = _oracle_rows(golden_scene(name), kernel == "runBVGPU")
+        assert np.array_equal(got, want), (key, int((got != want).sum()))
+
+
+def test_planted_oracle_mistake_is_caught(oracle_lib, tmp_path):
+    """A convention slip that keeps the statistics -- discRay's point with sin and
+    cos swapped (RayFactorGPU.cl:304-309) -- fails the per-ray pin."""
+    from oracle import build as B
+    bad = O.load_variant(B.build_oracle_variant(tmp_path / "librf_oracle_planted.so",
+                                                ["RFO_PLANTED_DISC_SWAP"]))
+    ref = _ref_rays()
+    sc = golden_scene("gen_enclosure3")  # two disc emitters
+    got = _oracle_rows(sc, False, lib_=bad)
+    want = ref["gen_enclosure3:runGPU"]
+    disc_rows = [e for e in range(sc.n) if int(sc.primitives[e]["type"]) == 5]
+    assert disc_rows and not np.array_equal(got[disc_rows], want[disc_rows])
+    other = [e for e in range(sc.n) if e not in disc_rows]
+    assert np.array_equal(got[other], want[other])
+
+
+def test_oracle_equals_compiled_reference_kernel_more_rays(oracle_lib):
+    """Wider windows straight against the reference kernel compiled here (needs the
+    reference checkout; the committed fixture above covers the rest)."""
+    from oracle import build as B
+    if not B.reference_present():
+        pytest.skip("reference checkout not present")
+    B.build_ref()
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    MG = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(MG)
+    from helpers import SAMPLE_NAMES, GEN_NAMES
+    lib = MG.load_ref_kernel()
+    rng = np.random.default_rng(5)
+    for name in SAMPLE_NAMES + GEN_NAMES:
+        sc = golden_scene(name)
+        g0 = int(rng.integers(8, 1 << 30))
+        windows = ((g0, g0 + 24),)
+        for use_bv in ([0, 1] if sc.bounding_volumes.shape[0] else [0]):
+            want = MG.ref_kernel_rays(lib, sc, use_bv, windows)
+            got = np.stack([O.trace_rays(sc, O.params(use_bv=use_bv), e, 4 * g0, 4 * (g0 + 24))
+                            for e in range(sc.n)])
+            assert np.array_equal(got, want), (name, use_bv, int((got != want).sum()))
