@@ -42,7 +42,6 @@ constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 32768
 constexpr int kDirGrid = 16;                                     // octahedral direction cells per axis
 constexpr int kOrigCells = 16;                                   // emission-parameter cells (4 x 4)
 constexpr int kCells = kDirGrid * kDirGrid * kOrigCells;         // 4096 sort keys
-constexpr int kBatchTile = 512;                                  // scenes up to this stay in smem
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
 constexpr int kBruteMax = 12;                                    // scenes up to this are not culled
 constexpr float kCondRel = 16.0f / 8388608.0f;                   // 16 ulps of the terms

@@ -400,10 +400,13 @@ float scene_eps(float eps, const float4 *bs, int n)
 }  // namespace
 
 // Mixed-precision tables of one scene as the batched kernel reads them
-// (re-centred transforms, hit records, bounding spheres with squared radius).
-void rf::prepare_mixed_tables(const rf_primitive *prims, int n, rf_primitive *emit, HitRec *tab, float4 *bs)
+// (re-centred transforms, hit records, bounding spheres with squared radius)
+// and the scene's self-hit threshold (eps < 0: relative, as rf_trace forms it).
+void rf::prepare_mixed_tables(const rf_primitive *prims, int n, float eps, rf_primitive *emit, HitRec *tab,
+                              float4 *bs, float *eps_out)
 {
     prepare_mixed(prims, n, emit, tab, bs);
+    *eps_out = scene_eps(eps, bs, n);
     for (int i = 0; i < n; ++i) bs[i] = widen_sq(bs[i]);
 }
 

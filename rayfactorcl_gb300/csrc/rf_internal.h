@@ -94,11 +94,14 @@ cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, int gr
 int batched_blocks_per_sm(bool rec, bool resident);
 size_t batched_smem_bytes();
 int batched_tile();  // scenes with at most this many surfaces use the resident kernel
+constexpr int kBatchTile = 512;  // surfaces the resident kernel keeps in shared memory
 constexpr int kBatchMaxSurfaces = 32767;  // nearest hits are kept as int16 in shared memory
 constexpr int kBatchChunkDraws = 8192;  // Philox draws per chunk of the batched kernel
 
-// Host preparation of one scene for the batched kernel (rf_capi.cu).
-void prepare_mixed_tables(const rf_primitive *prims, int n, rf_primitive *emit, HitRec *tab, float4 *bs);
+// Host preparation of one scene for the batched kernel (rf_capi.cu); eps_out
+// receives the scene's self-hit threshold for the configured eps.
+void prepare_mixed_tables(const rf_primitive *prims, int n, float eps, rf_primitive *emit, HitRec *tab, float4 *bs,
+                          float *eps_out);
 
 // FP64 post-processing and probes (rf_kern_post.cu).
 cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,

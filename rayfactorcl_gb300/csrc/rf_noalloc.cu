@@ -24,6 +24,9 @@ using namespace rf;
 namespace {
 
 constexpr int kMaxPrims = RF_NOALLOC_MAX_PRIMS;
+// the call always launches the kernel variant that keeps the scene's tables in
+// shared memory, which holds kBatchTile surfaces
+static_assert(kMaxPrims <= kBatchTile, "RF_NOALLOC_MAX_PRIMS must fit the resident kernel's tables");
 constexpr int kMaxDevices = 128;
 
 // Layout of the scratch array.
@@ -73,7 +76,7 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
 {
     if (!prims || !rays || !hits_dev || n <= 0) return RF_ERR_INVALID_ARG;
     if (n > kMaxPrims) return RF_ERR_OVERFLOW;  // the scratch array holds RF_NOALLOC_MAX_PRIMS surfaces
-    if (!(eps >= 0.0f) || !std::isfinite(eps)) return RF_ERR_INVALID_ARG;
+    if (!std::isfinite(eps)) return RF_ERR_INVALID_ARG;
     for (int i = 0; i < n; ++i) {
         const rf_primitive &p = prims[i];
         if (p.type < 0 || p.type > RF_DISC || !finite12(p.m) || !finite12(p.invm)) return RF_ERR_BAD_SCENE;
@@ -96,7 +99,8 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     }
     unsigned char *base = g_dev[dev];
 
-    prepare_mixed_tables(prims, n, h_emit, h_tab, h_sph);
+    float seps = eps;  // eps < 0: relative to the scene's size, like rf_trace
+    prepare_mixed_tables(prims, n, eps, h_emit, h_tab, h_sph, &seps);
     int nseg = 0;
     int64_t chunks = 0;
     for (int e = 0; e < n; ++e) {
@@ -115,7 +119,7 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     si.n = n;
     si.prim_off = 0;
     si.hits_off = 0;
-    si.eps = eps;
+    si.eps = seps;
 
     // copies from pageable host memory return once the source has been staged,
     // so the static host tables may be refilled by the next caller
@@ -147,7 +151,7 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     p.compat = compat;
     p.key1 = key1;
     p.scene_id = 0;
-    p.eps = eps;
+    p.eps = seps;
     int bps = batched_blocks_per_sm(false, true);
     if (bps <= 0) bps = 1;
     const int grid = (int)(chunks < (int64_t)sms * bps ? chunks : (int64_t)sms * bps);

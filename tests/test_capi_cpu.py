@@ -3,7 +3,6 @@ declares, the header compiles as C and C++ with the reference's struct sizes, th
 integration shim compiles against the reference's own Scene.h, and the host-side
 rules (budgets, output format, validation) behave as the reference does."""
 import ctypes
-import os
 import re
 import subprocess
 from pathlib import Path
@@ -18,7 +17,7 @@ from rayfactorcl_gb300.scene import BV_DTYPE, PRIM_DTYPE, parse_scene_xml
 
 ROOT = Path(__file__).resolve().parent.parent
 HEADER = ROOT / "include" / "rayfactor_gb300.h"
-REFERENCE = Path(os.environ.get("RF_REFERENCE_DIR", "/root/reference"))
+from oracle.build import REFERENCE  # noqa: E402  (RF_REFERENCE_DIR, else ../reference)
 
 
 def _declared():
@@ -66,21 +65,70 @@ int main(void) { printf("%d %d %d", (int)sizeof(rf_primitive), (int)sizeof(rf_bo
     assert PRIM_DTYPE.itemsize == 112 and BV_DTYPE.itemsize == 72
 
 
-def test_integration_shim_compiles_against_reference_scene(tmp_path):
-    """The runCL_GPURNG replacement of INTEGRATION.md, compiled with the reference's
-    Scene.h, TinyXML-2 and affine headers (syntax and layout checks only)."""
-    rfc = REFERENCE / "RayFactorCL"
-    if not (rfc / "Scene.h").exists():
-        pytest.skip("reference checkout not present")
-    md = (ROOT / "INTEGRATION.md").read_text()
-    shim = md.split("```cpp", 1)[1].split("```", 1)[0]
-    src = '#include <cstdio>\n#include "Scene.h"\n' + shim
-    f = tmp_path / "shim.cpp"
-    f.write_text(src)
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-w", "-I", str(HEADER.parent), "-I", str(rfc),
-                        "-I", str(rfc / "TinyXML-2"), "-I", str(rfc / "Affine Transformation"), str(f)],
-                       capture_output=True, text=True)
+SHIM_DIR = ROOT / "tests" / "shim"
+
+
+def build_shim_program(out: Path, stub: bool, lib: Path) -> Path:
+    """tests/shim/shim_main.cpp + include/rayfactor_gb300_shim.hpp linked with the
+    library: with the reference's own Scene/TinyXML-2/affine sources (stub=False)
+    or with the test stand-in tests/shim/scene_stub.h (stub=True)."""
+    cmd = ["g++", "-std=c++17", "-O1", "-w", "-I", str(HEADER.parent), "-I", str(SHIM_DIR)]
+    srcs = [str(SHIM_DIR / "shim_main.cpp")]
+    if stub:
+        cmd.append("-DRF_SHIM_SCENE_STUB")
+    else:
+        rfc = REFERENCE / "RayFactorCL"
+        aff, txml = rfc / "Affine Transformation", rfc / "TinyXML-2"
+        cmd += ["-I", str(rfc), "-I", str(aff), "-I", str(txml)]
+        srcs += [str(rfc / "Scene.cpp"), str(txml / "tinyxml2.cpp"), str(aff / "AffineTransformation.cpp"),
+                 str(aff / "Matrices.cpp")]
+    cmd += ["-o", str(out), *srcs, "-L", str(lib.parent), "-lrayfactor_gb300",
+            "-Wl,-rpath," + str(lib.parent)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+    return out
+
+
+def _run_shim(exe: Path, scene_arg: Path, cwd: Path):
+    return subprocess.run([str(exe), str(scene_arg)], capture_output=True, text=True, cwd=cwd, timeout=600)
+
+
+def _gpu_present() -> bool:
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    st = L.rf_create(ctypes.byref(h), None)
+    if st == 0:
+        L.rf_destroy(h)
+    return st == 0
+
+
+def test_shim_links_with_reference_scene_loader(built_lib, tmp_path):
+    """The drop-in for runCL_GPURNG (include/rayfactor_gb300_shim.hpp) compiled and
+    linked with the reference's own Scene.cpp, TinyXML-2 and affine code and the
+    library, then run as the reference's main() on a sample scene: it reads the XML
+    with the reference loader and calls the C ABI.  Without a GPU the call must come
+    back with the library's no-device error, not an exit or a crash."""
+    rfc = REFERENCE / "RayFactorCL"
+    if not (rfc / "Scene.cpp").exists():
+        pytest.skip("reference checkout not present")
+    exe = build_shim_program(tmp_path / "shim_ref", False, built_lib)
+    r = _run_shim(exe, REFERENCE / "sample-geometries" / "input-C47.xml", tmp_path)
+    if _gpu_present():
+        assert r.returncode == 0 and (tmp_path / "output.txt").exists(), r.stderr
+    else:
+        assert r.returncode == 1 and "rayfactor_gb300: no CUDA device" in r.stderr, (r.returncode, r.stderr)
+        assert not (tmp_path / "output.txt").exists()
+
+
+def test_shim_builds_with_scene_stand_in(built_lib, tmp_path):
+    """The same program with the test stand-in Scene (used by the GPU test where the
+    reference checkout is absent) builds and reaches the C ABI."""
+    exe = build_shim_program(tmp_path / "shim_stub", True, built_lib)
+    r = _run_shim(exe, ROOT / "tests" / "golden" / "scenes" / "input-C47.bin", tmp_path)
+    if _gpu_present():
+        assert r.returncode == 0, r.stderr
+    else:
+        assert r.returncode == 1 and "no CUDA device" in r.stderr, r.stderr
 
 
 def _budgets(sc, n_samples, compat):
