@@ -284,8 +284,13 @@ def run_ours(args):
     hits = np.zeros((sc.n, sc.n), np.uint64)
     t.read_results(hits, None)
     assert int(hits.sum()) <= total_rays
-    work = t.work_counts() if headline == PREC_MIXED else None
     refined = t.refined_count() if headline == PREC_MIXED else 0
+    work = None
+    if headline == PREC_MIXED:  # the timed kernel does not count; one more run that does
+        with Tracer(precision=headline, key1=w.key1, device=local, work_counts=True) as tc:
+            tc.set_scene(sc)
+            tc.trace(rays)
+            work = tc.work_counts()
     if world > 1:
         import torch.distributed as dist
         m = torch.tensor([ms_step], device=dev)

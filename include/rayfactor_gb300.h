@@ -103,7 +103,11 @@ typedef struct rf_config {
     int32_t table_mode;   /* 0: autotuned / default; 1: surfaces staged in shared memory; 2: read through L1 */
     int32_t test_order;   /* 0: autotuned / default; 1: a thread's 4 or 8 rays tested together against
                            * each surface; 2: one ray at a time against all surfaces (smaller code) */
-    uint32_t reserved[4];
+    int32_t work_counts;  /* RF_PREC_MIXED: 1 = the batched kernel also counts its tests for
+                           * rf_last_work_counts (a few per cent slower); 0 = no counting      */
+    int32_t batched_grid; /* RF_PREC_MIXED: 0 = one persistent block per SM; > 0 = at most this
+                           * many blocks (results do not depend on it)                         */
+    uint32_t reserved[2];
 } rf_config;
 
 typedef struct rf_ctx rf_ctx;
@@ -271,11 +275,13 @@ rf_status rf_get_launch_config(rf_ctx *ctx, int32_t *block, int32_t *rays_per_th
 /* (No counterpart in the reference.)  Counters of the last mixed-precision run: tests re-evaluated in FP64. */
 rf_status rf_last_refine_count(rf_ctx *ctx, uint64_t *refined_tests);
 
-/* (No counterpart in the reference.)  Work of the last mixed-precision run: counts[0..5] ray x surface tests
+/* (No counterpart in the reference.)  Work of the last mixed-precision run made with
+ * rf_config.work_counts = 1 (zeros otherwise): counts[0..5] ray x surface tests
  * performed by surface type (RF_CYLINDER..RF_DISC), counts[6] candidate
- * surfaces per packet that passed the packet's cone test (each then checked ray
- * by ray), counts[7] ray packets (32 rays).  Tests skipped by culling are the
- * all-pairs count minus the sum of counts[0..5]. */
+ * surfaces of the packets (the union of their rays' cell masks, or the surfaces
+ * their bounds can reach; each then checked ray by ray), counts[7] ray packets
+ * (32 rays).  Tests skipped by culling are the all-pairs count minus the sum of
+ * counts[0..5]. */
 rf_status rf_last_work_counts(rf_ctx *ctx, uint64_t *counts);
 
 /* (No counterpart in the reference.)  FP32 issue-rate probe: dependent-FMA throughput of the device in FMA/s

@@ -44,7 +44,8 @@ class RfConfig(ctypes.Structure):
                 ("device", ctypes.c_int32), ("block_size", ctypes.c_int32),
                 ("rays_per_thread", ctypes.c_int32), ("scene_id", ctypes.c_uint32),
                 ("tally_mode", ctypes.c_int32), ("table_mode", ctypes.c_int32),
-                ("test_order", ctypes.c_int32), ("reserved", ctypes.c_uint32 * 4)]
+                ("test_order", ctypes.c_int32), ("work_counts", ctypes.c_int32),
+                ("batched_grid", ctypes.c_int32), ("reserved", ctypes.c_uint32 * 2)]
 
 
 class RfSceneDesc(ctypes.Structure):

@@ -6,30 +6,37 @@
 // atomic counter), so scenes of 10 and of 400 surfaces load-balance.
 //
 // Per chunk (32768 rays) a block
-//   1. emits every ray with FP32 hardware approximations (same streams and
-//      emission formulas as the plain kernel, RayFactorGPU.cl:298-443) only to
-//      compute its sort key: octahedral direction cell (16x16, Morton order)
-//      above a 4x4 cell of the two surface parameters of the emission point,
+//   1. draws every Philox word once, keeps its 24 significant bits in shared
+//      memory (12 bytes per draw) and emits every ray with FP32 hardware
+//      approximations (same streams and emission formulas as the plain kernel,
+//      RayFactorGPU.cl:298-443) only to compute its sort key: octahedral
+//      direction cell (16x16, Morton order) above a 4x4 cell of the two surface
+//      parameters of the emission point,
 //   2. counting-sorts the ray indices by key in shared memory,
 //   3. lets its warps take packets of 32 sorted rays from a shared counter; each
-//      lane re-emits its ray from the stream (keys and indices are all that a
-//      chunk keeps, so chunks are 8x larger than stored rays would allow and
-//      packets are tighter).  The packet's origin ball and direction cone are
-//      reduced across the warp; then each lane checks the cone against a
-//      different surface's bounding sphere, 32 surfaces per pass, and a ballot
-//      gives the packet's candidate surfaces.  For each candidate (in index
-//      order) every lane checks its own ray against the sphere, and the full
-//      test runs only if some lane's ray can reach it,
+//      lane re-emits its ray from the stored uniforms.  The packet's candidate
+//      surfaces are the union of its rays' cell masks (built once per scene by
+//      build_masks_kernel: every surface that some ray of that emitter, cell and
+//      parameter patch can reach), or, for scenes without masks, the surfaces
+//      whose bounding sphere the packet's origin ball and direction cone can
+//      reach.  For each candidate (in index order) every lane checks its own ray
+//      against the surface's bounding sphere and its own cell's mask bit, and
+//      the full test runs only if some lane passes,
 //   4. evaluates the surviving tests in FP32, with quadric discriminants in
 //      cancellation-free forms; a discriminant within 16 rounding errors of
 //      its terms (a grazing ray), or a cone whose A lost 12 bits, is
-//      re-evaluated in FP64 after the packet (counted), and
-//   5. tallies first hits in a shared-memory row histogram flushed as 64-bit
-//      atomics whenever the (scene, emitter) row changes.
-// Skipping a surface whose bounding sphere no ray of the packet can reach does
-// not change any ray's nearest hit; only the arithmetic differs from the
-// exact kernel.  Scenes of at most kBruteMax surfaces skip steps 1-3: every
-// thread tests its own rays against all surfaces (culling cannot pay there).
+//      re-evaluated in FP64 after the packet, and
+//   5. tallies first hits in a shared-memory row histogram (flushed as 64-bit
+//      atomics whenever the (scene, emitter) row changes) straight from the
+//      packet loop.
+// A lane keeps a test's result only when its own checks passed (step 3), so a
+// ray's result depends on the ray alone, never on the rays it shares a packet
+// with: the per-lane gate is a function of the ray (its cell mask bit and its
+// sphere check), and every surface that passes it is tested because its mask
+// bit puts it among the packet's candidates.  Skipping a surface that the
+// ray cannot reach does not change its nearest hit; only the arithmetic
+// differs from the exact kernel.  Scenes of at most kBruteMax surfaces skip
+// steps 1-3: every thread tests its own rays against all surfaces.
 #pragma once
 
 #include "rf_device.cuh"
@@ -38,22 +45,27 @@ namespace rf {
 
 constexpr int kBatchThreads = 1024;
 constexpr int kBatchDraws = 8;                                   // draws per thread per chunk
-constexpr int kChunkRays = kBatchThreads * kBatchDraws * 4;      // 32768
+constexpr int kChunkDraws = kBatchThreads * kBatchDraws;         // 8192
+constexpr int kChunkRays = kChunkDraws * 4;                      // 32768
 constexpr int kDirGrid = 16;                                     // octahedral direction cells per axis
 constexpr int kOrigCells = 16;                                   // emission-parameter cells (4 x 4)
 constexpr int kCells = kDirGrid * kDirGrid * kOrigCells;         // 4096 sort keys
 constexpr int kBatchHist = 512;                                  // rows up to this stay in smem
-constexpr int kBruteMax = 12;                                    // scenes up to this are not culled
+constexpr int kBruteMax = kBatchBruteMax;                        // scenes up to this are not culled
 constexpr float kCondRel = 16.0f / 8388608.0f;                   // 16 ulps of the terms
 constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost in a cone's A
 static_assert(kCells == 4 * kBatchThreads, "the bucket scan gives each thread four buckets");
+static_assert(kCells == kMaskCells, "one mask per sort key");
+static_assert(kChunkRays <= 65536, "ray indices of a chunk are 16-bit");
 
-// Rays are not stored: emission computes each ray's sort key, and the lane that
-// traces a ray re-emits it from its stream (a Philox draw and the emission
-// formulas), so a chunk costs two bytes of key and two of permutation per ray.
+// Rays are not stored: the lane that traces a ray re-emits it from its draw's
+// uniforms, kept as 4 x 24 bits in three words (u01 uses only the top 24 bits of
+// each Philox word, RayFactorGPU.cl:59-62), so a chunk costs 12 bytes per draw
+// and two bytes of permutation per ray.  Until the sort the permutation array
+// holds each ray's key.
 struct BatchSmem {
-    uint16_t perm[kChunkRays];          // sorted position -> local ray index
-    int16_t keyres[kChunkRays];         // sort key by local ray index, then nearest surface by sorted position
+    uint16_t perm[kChunkRays];          // key by local ray index, then sorted position -> local ray index
+    uint32_t unif[3][kChunkDraws];      // the draws' 24-bit uniforms, packed
     __align__(16) int cnt[kCells];      // bucket sizes, then running bucket offsets
     int wsum[kBatchThreads / 32];
     HitRec tab[kBatchTile];
@@ -64,8 +76,30 @@ struct BatchSmem {
     int next_packet;
     int n_valid;
     unsigned long long work[8];
-    uint32_t wcount[kBatchThreads / 32][8];  // per warp: tests by type, sphere checks, packets
+    uint32_t wcount[kBatchThreads / 32][8];  // per warp: tests by type, candidates, packets (COUNT)
 };
+
+// The top 24 bits of the four Philox words of a draw in three words, and back
+// as the four uniforms of u01_closed_open_4x32_24 (RayFactorGPU.cl:59-62).
+__device__ __forceinline__ void pack_uniforms(uint4 u, uint32_t &w0, uint32_t &w1, uint32_t &w2)
+{
+    const uint32_t a = u.x >> 8, b = u.y >> 8, c = u.z >> 8, d = u.w >> 8;
+    w0 = a | (b << 24);
+    w1 = (b >> 8) | (c << 16);
+    w2 = (c >> 16) | (d << 8);
+}
+
+__device__ __forceinline__ void unpack_uniforms(uint32_t w0, uint32_t w1, uint32_t w2, float uf[4])
+{
+    const uint32_t a = w0 & 0xffffffu;
+    const uint32_t b = __funnelshift_r(w0, w1, 24) & 0xffffffu;
+    const uint32_t c = __funnelshift_r(w1, w2, 16) & 0xffffffu;
+    const uint32_t d = w2 >> 8;
+    uf[0] = __fmul_rn(__uint2float_rn(a), 0x1p-24f);
+    uf[1] = __fmul_rn(__uint2float_rn(b), 0x1p-24f);
+    uf[2] = __fmul_rn(__uint2float_rn(c), 0x1p-24f);
+    uf[3] = __fmul_rn(__uint2float_rn(d), 0x1p-24f);
+}
 
 // Octahedral cell of a direction, kDirGrid x kDirGrid cells in Morton order.
 __device__ __forceinline__ int direction_cell(float x, float y, float z)
@@ -298,15 +332,34 @@ __device__ __noinline__ float hit_f64(const HitRec &h, const Ray<float> &w, floa
     }
 }
 
-// Full nearest-hit search for one ray with FP64 for every ill-conditioned
-// quadric (cold path: the ray deferred more than one test, and a lane keeps
-// only one).
+// Sort key of a ray: its direction cell above the 4 x 4 cell of the two surface
+// parameters (r[0], r[1]) of its emission point.
+__device__ __forceinline__ int ray_key(const Ray<float> &ray, const float r[4])
+{
+    return (direction_cell(ray.cx, ray.cy, ray.cz) << 4) | (min(3, (int)(r[0] * 4.0f)) << 2) |
+           min(3, (int)(r[1] * 4.0f));
+}
+
+// The lane's own gate for surface j: its cell's mask bit (when the scene has
+// masks) and its ray's bounding-sphere check.
+__device__ __forceinline__ bool own_gate(const uint32_t *mcell, int j, const Ray<float> &ray, float idd,
+                                         const float4 b)
+{
+    if (mcell && !((__ldg(mcell + (j >> 5)) >> (j & 31)) & 1u)) return false;
+    return ray_may_hit(ray, idd, b);
+}
+
+// Full nearest-hit search for one ray over the surfaces its gate admits, with
+// FP64 for every ill-conditioned quadric (cold path: the ray deferred more than
+// one test, and a lane keeps only one).
 __device__ __noinline__ int retrace_f64(int n, bool resident, const HitRec *stab, const HitRec *gtab,
-                                        const Ray<float> &ray, float eps, bool sc)
+                                        const float4 *sbs, const float4 *gbs, const uint32_t *mcell,
+                                        const Ray<float> &ray, float idd, float eps, bool sc)
 {
     float tb = MFast::inf();
     int bi = -1;
     for (int j = 0; j < n; ++j) {
+        if (!own_gate(mcell, j, ray, idd, resident ? sbs[j] : __ldg(gbs + j))) continue;
         const HitRec h = resident ? stab[j] : load_rec(gtab, j);
         bool defer = false;
         float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
@@ -317,8 +370,10 @@ __device__ __noinline__ int retrace_f64(int n, bool resident, const HitRec *stab
 }
 
 // RESIDENT: every scene of the launch fits the shared-memory tables
-// (n <= kBatchTile); otherwise surfaces are read through L1.
-template <bool REC, bool RESIDENT>
+// (n <= kBatchTile); otherwise surfaces are read through L1.  COUNT: also count
+// the tests by surface type, the candidates and the packets (p.work); the
+// counters cost a few per cent, so timed runs leave them out.
+template <bool REC, bool RESIDENT, bool COUNT>
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TraceParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -332,13 +387,14 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
     int cur_scene = -1, cur_emitter = -1;
     SceneInfo si{};
     int nref = 0;
-    // work counters: per warp in shared memory (lane 0; tests by type in the
-    // registers of lanes 0-5), folded per chunk into the block's 64-bit counters
-    if (tid < 8) S.work[tid] = 0ull;
-    if (lane < 8) S.wcount[warp][lane] = 0u;
+    if (COUNT) {
+        if (tid < 8) S.work[tid] = 0ull;
+        if (lane < 8) S.wcount[warp][lane] = 0u;
+    }
     bool hist_on = false;
     int row_chunks = 0;   // chunks tallied into the shared-memory row since its last flush
-    uint32_t tcount = 0;  // lane t < 6: lane-tests of surfaces of type t by this warp (this chunk)
+    uint32_t tcount = 0;  // COUNT, lane t < 6: lane-tests of surfaces of type t by this warp (this chunk)
+    const uint32_t *mrow = nullptr;  // cell masks of the current row (null: packet bounds instead)
 
     auto flush = [&]() {
         __syncthreads();
@@ -353,6 +409,18 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
             }
         }
         __syncthreads();
+    };
+    auto fold_counts = [&]() {
+        if (COUNT) {
+            if (lane < 6) S.wcount[warp][lane] += tcount;
+            tcount = 0;
+            __syncwarp();
+            if (lane < 8) {
+                const uint32_t v = S.wcount[warp][lane];
+                if (v) atomicAdd(&S.work[lane], (unsigned long long)v);
+                S.wcount[warp][lane] = 0u;
+            }
+        }
     };
 
     for (;;) {
@@ -388,13 +456,19 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 reinterpret_cast<float *>(&S.emit)[tid] =
                     reinterpret_cast<const float *>(p.emit + si.prim_off + sg.emitter)[tid];
             cur_emitter = sg.emitter;
+            mrow = nullptr;
+            if (p.mask_off) {
+                const int64_t mo = p.mask_off[si.prim_off + sg.emitter];
+                if (mo >= 0) mrow = p.cmask + mo;
+            }
         }
         for (int i = tid; i < kCells; i += blockDim.x) S.cnt[i] = 0;
         if (tid == 0) S.next_packet = 0;
         __syncthreads();
-        const int64_t gid0 = (sg.ray_begin >> 2) + (c - sg.chunk_begin) * (int64_t)(kBatchThreads * kBatchDraws);
+        const int64_t gid0 = (sg.ray_begin >> 2) + (c - sg.chunk_begin) * (int64_t)kChunkDraws;
         const uint32_t sid = (p.compat & RF_COMPAT_STREAMS) ? 0u : (p.scene_id + (uint32_t)sg.scene);
         const HitRec *gtab = p.tab + si.prim_off;
+        unsigned long long *grow = p.hits + si.hits_off + (int64_t)cur_emitter * si.n;
 
         if (si.n <= kBruteMax) {  // block-uniform: too few surfaces for culling to pay
             // every thread traces its own rays against all surfaces in index order
@@ -432,65 +506,70 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
                             ++nref;
                         } else if (dj == -2) {
-                            bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, ray, eps, sc);
+                            bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, S.bs, p.bsph + si.prim_off, nullptr, ray,
+                                             MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz), eps, sc);
                             nref += 2;
                         }
                     }
-                    nv_warp += __popc(__ballot_sync(0xffffffffu, valid));
+                    // all 32 lanes reach the warp-wide calls below
+                    if (COUNT) nv_warp += __popc(__ballot_sync(0xffffffffu, valid));
                     if (REC) {
                         if (valid) p.rec[gid0 * 4 + 4 * d + v - p.rec_base] = bi;
                     } else if (hist_on) {
                         warp_tally(S.hist, bi);
                     } else {
-                        warp_tally_global(p.hits + si.hits_off + (int64_t)cur_emitter * si.n, bi);
+                        warp_tally_global(grow, bi);
                     }
                 }
             }
-            if (lane == 0 && nv_warp)
-                for (int j = 0; j < si.n; ++j) {
-                    const int type = RESIDENT ? __float_as_int(S.tab[j].aux.x) : __float_as_int(__ldg(&gtab[j].aux.x));
-                    if ((unsigned)type < 6u) S.wcount[warp][type] += nv_warp;
-                }
-            __syncwarp();
-            if (lane < 8) {
-                const uint32_t cnt = S.wcount[warp][lane];
-                if (cnt) atomicAdd(&S.work[lane], (unsigned long long)cnt);
-                S.wcount[warp][lane] = 0u;
+            if (COUNT) {
+                if (lane == 0 && nv_warp)
+                    for (int j = 0; j < si.n; ++j) {
+                        const int type = RESIDENT ? __float_as_int(S.tab[j].aux.x) : __float_as_int(__ldg(&gtab[j].aux.x));
+                        if ((unsigned)type < 6u) S.wcount[warp][type] += nv_warp;
+                    }
+                fold_counts();
             }
             __syncthreads();
             continue;
         }
 
-        // 1. sort keys (draw d = g*blockDim + tid, ray l = 4d + v): direction cell
-        // (Morton) above the 4 x 4 cell of the surface parameters (r[0], r[1])
+        // 1. uniforms and sort keys (draw d = g*blockDim + tid, ray l = 4d + v);
+        // keys go to perm[l] until the sort
 #pragma unroll 1
         for (int g = 0; g < kBatchDraws; ++g) {
             const int d = g * kBatchThreads + tid;
             const int64_t gid = gid0 + d;
-            if (gid * 4 + 3 < sg.ray_begin || gid * 4 >= sg.ray_end) {  // no ray of this draw
-                *reinterpret_cast<uint2 *>(&S.keyres[4 * d]) = make_uint2(0x10001000u, 0x10001000u);  // kCells
-                continue;
-            }
-            const uint4 u = stream_bits(p.compat, p.key1, sid, sg.emitter, gid);
-            const float uf[4] = {u01(u.x), u01(u.y), u01(u.z), u01(u.w)};
+            uint2 kk = make_uint2(kCells | (kCells << 16), kCells | (kCells << 16));  // no valid ray
+            if (gid * 4 + 3 >= sg.ray_begin && gid * 4 < sg.ray_end) {
+                const uint4 u = stream_bits(p.compat, p.key1, sid, sg.emitter, gid);
+                pack_uniforms(u, S.unif[0][d], S.unif[1][d], S.unif[2][d]);
+                const float uf[4] = {u01(u.x), u01(u.y), u01(u.z), u01(u.w)};
+                int key4[4];
 #pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                float r[4];
+                for (int v = 0; v < 4; ++v) {
+                    float r[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
-                const Ray<float> ray = emit_ray<MFast>(S.emit, r);
-                const int64_t rid = gid * 4 + v;
-                const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
-                const int key = valid ? (direction_cell(ray.cx, ray.cy, ray.cz) << 4) |
-                                            (min(3, (int)(r[0] * 4.0f)) << 2) | min(3, (int)(r[1] * 4.0f))
-                                      : kCells;
-                S.keyres[4 * d + v] = (int16_t)key;
-                if (valid) atomicAdd(&S.cnt[key], 1);
+                    for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
+                    const Ray<float> ray = emit_ray<MFast>(S.emit, r);  // the origin is dead code here
+                    const int64_t rid = gid * 4 + v;
+                    const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
+                    key4[v] = valid ? ray_key(ray, r) : kCells;
+                    if (valid) atomicAdd(&S.cnt[key4[v]], 1);
+                }
+                kk = make_uint2((uint32_t)key4[0] | ((uint32_t)key4[1] << 16),
+                                (uint32_t)key4[2] | ((uint32_t)key4[3] << 16));
             }
+            *reinterpret_cast<uint2 *>(&S.perm[4 * d]) = kk;
         }
         __syncthreads();
+        uint2 mykeys[kBatchDraws];
+#pragma unroll
+        for (int g = 0; g < kBatchDraws; ++g)
+            mykeys[g] = *reinterpret_cast<const uint2 *>(&S.perm[4 * (g * kBatchThreads + tid)]);
         // 2. counting sort: block-wide exclusive scan of the bucket sizes (four
-        // consecutive buckets per thread), then each ray claims a slot of its bucket
+        // consecutive buckets per thread), then each ray claims a slot of its
+        // bucket (in any order: a ray's result does not depend on its packet)
         {
             const int4 c4 = *reinterpret_cast<const int4 *>(&S.cnt[4 * tid]);
             const int sum = c4.x + c4.y + c4.z + c4.w;
@@ -519,25 +598,28 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 make_int4(run, run + c4.x, run + c4.x + c4.y, run + c4.x + c4.y + c4.z);
         }
         __syncthreads();
-#pragma unroll 1
+#pragma unroll
         for (int g = 0; g < kBatchDraws; ++g) {
             const int d = g * kBatchThreads + tid;
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
-                const int key = S.keyres[4 * d + v];
+                const uint32_t w = (v < 2) ? mykeys[g].x : mykeys[g].y;
+                const int key = (int)((w >> (16 * (v & 1))) & 0xffffu);
                 if (key < kCells) S.perm[atomicAdd(&S.cnt[key], 1)] = (uint16_t)(4 * d + v);
             }
         }
         __syncthreads();
         const int n_valid = S.n_valid;
 
-        // 3-4. warps take packets of 32 sorted rays; 32 surfaces per pass are
-        // prefiltered against the packet's cone, candidates get per-ray sphere
-        // checks and, if any lane can reach them, the full test (index order, so
-        // ties go to the lower index as in RayFactorGPU.cl:463-467)
+        // 3-5. warps take packets of 32 sorted rays; candidates are the union of
+        // the rays' cell masks (or the surfaces the packet's bounds can reach);
+        // each candidate gets the lanes' own gates and, if any lane passes, the
+        // full test (index order, so ties go to the lower index as in
+        // RayFactorGPU.cl:463-467); first hits are tallied at once
         constexpr bool resident = RESIDENT;
         const float4 *gbs = p.bsph + si.prim_off;
         const int n_packets = (n_valid + 31) >> 5;
+        const int nwords_all = (si.n + 31) >> 5;
         for (;;) {
             int k = 0;
             if (lane == 0) k = atomicAdd(&S.next_packet, 1);
@@ -545,37 +627,31 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
             if (k >= n_packets) break;  // warp-uniform
             const int pos = k * 32 + lane;
             const bool valid = pos < n_valid;
-            const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+            const int nvalid = COUNT ? __popc(__ballot_sync(0xffffffffu, valid)) : 0;  // every lane
             int bi = -1;
             {
-                const int nvalid = __popc(vmask);
                 // re-emit the lane's ray (an invalid lane traces the packet's first ray)
                 const int l = S.perm[valid ? pos : k * 32];
-                Ray<float> ray;
-                {
-                    const int v = l & 3;
-                    const uint4 u = stream_bits(p.compat, p.key1, sid, sg.emitter, gid0 + (l >> 2));
-                    const float uf[4] = {u01(u.x), u01(u.y), u01(u.z), u01(u.w)};
-                    float r[4];
+                const int d = l >> 2, v = l & 3;
+                float uf[4], r[4];
+                unpack_uniforms(S.unif[0][d], S.unif[1][d], S.unif[2][d], uf);
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const int q = (i + v + 1) & 3;
-                        r[i] = q == 0 ? uf[0] : (q == 1 ? uf[1] : (q == 2 ? uf[2] : uf[3]));
-                    }
-                    ray = emit_ray<MFast>(S.emit, r);
+                for (int i = 0; i < 4; ++i) {
+                    const int q = (i + v + 1) & 3;
+                    r[i] = q == 0 ? uf[0] : (q == 1 ? uf[1] : (q == 2 ? uf[2] : uf[3]));
                 }
+                const Ray<float> ray = emit_ray<MFast>(S.emit, r);
                 const float idd = MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
+                const uint32_t *mcell = mrow ? mrow + (int64_t)ray_key(ray, r) * nwords_all : nullptr;
                 float tb = MFast::inf();
                 int dj = -1, ndef = 0;  // deferred FP64 tests of this lane: the last one, and how many
-                if (lane == 0) S.wcount[warp][7] += 1;
-                // surfaces in blocks of 1024: phase A tests the packet's cone against 32
-                // spheres per pass and keeps one candidate word per lane; phase B walks the
-                // candidates in index order with the per-ray sphere vote and full test
+                if (COUNT && lane == 0) S.wcount[warp][7] += 1;
+                // surfaces in blocks of 1024 (one block when the scene has masks)
 #pragma unroll 1
                 for (int j0 = 0; j0 < si.n; j0 += 1024) {
                     const int nwords = min(32, (si.n - j0 + 31) >> 5);
-                    unsigned cmask = 0u;
-                    {
+                    unsigned cmask = 0u;  // without masks: lane w holds candidate word w
+                    if (!mcell) {  // block-uniform
                         const Packet pk = packet_bounds(ray, idd);
 #pragma unroll 1
                         for (int w = 0; w < nwords; ++w) {
@@ -586,41 +662,46 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             if (lane == w) cmask = cm;
                         }
                     }
-                    // lane w holds word w (0 beyond nwords): candidates of this block
-                    const unsigned ncand = __reduce_add_sync(0xffffffffu, (unsigned)__popc(cmask));
-                    if (lane == 0) S.wcount[warp][6] += ncand;
 #pragma unroll 1
                     for (int w = 0; w < nwords; ++w) {
-                        unsigned cm = __shfl_sync(0xffffffffu, cmask, w);
-                        const int jw = j0 + (w << 5) - 1;
+                        const int jw = j0 + (w << 5);
+                        unsigned mine, cm;
+                        if (mcell) {  // block-uniform
+                            mine = __ldg(mcell + (jw >> 5));
+                            cm = __reduce_or_sync(0xffffffffu, mine);
+                        } else {
+                            mine = 0xffffffffu;
+                            cm = __shfl_sync(0xffffffffu, cmask, w);
+                        }
+                        if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
                         // two candidates per pass: their sphere checks are independent
-                        // chains (latency hidden); tests still run in index order.  Lanes
-                        // past the end of the chunk repeat the packet's first ray, so
-                        // their votes change nothing.
-                        while (cm) {
-                            const int ja = jw + __ffs(cm);
+                        // chains (latency hidden); tests still run in index order
+                        while (cm) {  // cm is the same in every lane
+                            const int ba_ = __ffs(cm) - 1;
                             cm &= cm - 1;
-                            const int jb = cm ? jw + __ffs(cm) : -1;
+                            const int bb_ = cm ? __ffs(cm) - 1 : -1;
                             cm &= cm - 1;  // 0 stays 0
-                            const int jbs = jb >= 0 ? jb : ja;
-                            const float4 ba = resident ? S.bs[ja] : __ldg(gbs + ja);
-                            const float4 bb = resident ? S.bs[jbs] : __ldg(gbs + jbs);
-                            const bool ma = ray_may_hit(ray, idd, ba);
-                            const bool mb = jb >= 0 && ray_may_hit(ray, idd, bb);
+                            const int ja = jw + ba_, jb = jw + (bb_ >= 0 ? bb_ : ba_);
+                            const float4 sa = resident ? S.bs[ja] : __ldg(gbs + ja);
+                            const float4 sb = resident ? S.bs[jb] : __ldg(gbs + jb);
+                            const bool ma = ((mine >> ba_) & 1u) && ray_may_hit(ray, idd, sa);
+                            const bool mb = bb_ >= 0 && ((mine >> bb_) & 1u) && ray_may_hit(ray, idd, sb);
                             const unsigned va = __ballot_sync(0xffffffffu, ma);
                             const unsigned vb = __ballot_sync(0xffffffffu, mb);
 #pragma unroll
                             for (int q = 0; q < 2; ++q) {
-                                const int j = q ? jb : ja;
                                 if (!(q ? vb : va)) continue;  // warp-uniform
+                                const int j = q ? jb : ja;
+                                const bool gate = q ? mb : ma;
                                 const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
                                 const int type = __float_as_int(h.aux.x);
-                                tcount += lane == type ? nvalid : 0;
+                                if (COUNT) tcount += lane == type ? nvalid : 0;
                                 bool defer = false;
                                 const float t = hit_mixed(type, h, ray, eps, sc, defer);
-                                if (t < tb) { tb = t; bi = j; }
-                                ndef += defer;  // predicated, no branch
-                                dj = defer ? j : dj;
+                                if (gate && t < tb) { tb = t; bi = j; }
+                                const bool dg = gate && defer;
+                                ndef += dg;  // predicated, no branch
+                                dj = dg ? j : dj;
                             }
                         }
                     }
@@ -633,34 +714,17 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
                     ++nref;
                 } else if (valid && ndef > 1) {
-                    bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, ray, eps, sc);
+                    bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc);
                     nref += 2;
                 }
+                if (REC && valid) p.rec[gid0 * 4 + l - p.rec_base] = bi;
             }
-            S.keyres[pos] = (int16_t)bi;
-        }
-        if (lane < 6) S.wcount[warp][lane] += tcount;
-        tcount = 0;
-        __syncwarp();
-        if (lane < 8) {
-            const uint32_t v = S.wcount[warp][lane];
-            if (v) atomicAdd(&S.work[lane], (unsigned long long)v);
-            S.wcount[warp][lane] = 0u;
-        }
-        __syncthreads();
-        // 5. tally (or record) by sorted position; all rays of the chunk share one row
-        const int n_tally = (n_valid + 31) & ~31;  // whole warps (warp_tally needs every lane)
-        for (int pos = tid; pos < n_tally; pos += blockDim.x) {
-            const bool valid = pos < n_valid;
-            const int h = valid ? S.keyres[pos] : -1;
-            if (REC) {
-                if (valid) p.rec[gid0 * 4 + S.perm[pos] - p.rec_base] = h;
-            } else if (hist_on) {
-                warp_tally(S.hist, h);
-            } else {
-                warp_tally_global(p.hits + si.hits_off + (int64_t)cur_emitter * si.n, h);
+            if (!REC) {  // every lane: warp-aggregated tally
+                if (hist_on) warp_tally(S.hist, valid ? bi : -1);
+                else warp_tally_global(grow, valid ? bi : -1);
             }
         }
+        fold_counts();
         __syncthreads();
     }
     if (!REC) flush();
@@ -670,7 +734,76 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
     for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
     if (lane == 0 && tot && p.refined) atomicAdd(p.refined, (unsigned long long)tot);
     __syncthreads();
-    if (tid < 8 && p.work && S.work[tid]) atomicAdd(p.work + tid, S.work[tid]);
+    if (COUNT && tid < 8 && p.work && S.work[tid]) atomicAdd(p.work + tid, S.work[tid]);
+}
+
+// ---------------------------------------------------------------------------
+// Cell masks.  For a row (scene, emitter) and each of the kCells sort keys,
+// bit j of the key's mask says whether any ray of that emitter whose key it is
+// can reach surface j: origins in the parameter patch's ball (MaskInputs::patch,
+// 16 per emitter), directions in the direction cell's cone (cone[2*cell],
+// axis and cos in xyzw, sin in the next entry's x), surfaces covered by up to
+// kChainMax spheres (chain; radius < 0 ends the list) and, for planar surfaces,
+// the plane (plane.xyz unit normal, w = normal . point; w NaN: not planar), which
+// no ray crosses when the whole ball lies on one side and every direction of the
+// cone points away from it.  A ray from a ball B(c, rho) with a direction within
+// theta of axis a comes within R of a point C only if angle(C - c, a) <=
+// theta + asin((R + rho) / |C - c|).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool cell_reaches(float4 ball, float4 axis_cos, float sin_t, float4 sph)
+{
+    const float vx = sph.x - ball.x, vy = sph.y - ball.y, vz = sph.z - ball.z;
+    const float L2 = vx * vx + vy * vy + vz * vz;
+    const float R = (sph.w + ball.w) * 1.0001f + 1e-5f * sqrtf(L2) + 1e-7f;
+    if (L2 <= R * R) return true;
+    const float va = vx * axis_cos.x + vy * axis_cos.y + vz * axis_cos.z;
+    return va >= axis_cos.w * sqrtf(L2 - R * R) - sin_t * R;
+}
+
+__device__ __forceinline__ bool plane_separates(float4 ball, float4 axis_cos, float sin_t, float4 pl)
+{
+    if (!(pl.w == pl.w)) return false;  // not planar
+    const float h = pl.x * ball.x + pl.y * ball.y + pl.z * ball.z - pl.w;
+    const float na = pl.x * axis_cos.x + pl.y * axis_cos.y + pl.z * axis_cos.z;
+    const float margin = ball.w * 1e-4f + 1e-6f * (fabsf(pl.w) + ball.w) + 1e-7f;
+    if (h > ball.w + margin) return na >= sin_t + 1e-4f;     // every ray moves away on the + side
+    if (h < -(ball.w + margin)) return -na >= sin_t + 1e-4f; // ... or on the - side
+    return false;
+}
+
+__global__ void __launch_bounds__(256) build_masks_kernel(MaskInputs in, uint32_t *out)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= in.total_words) return;
+    int lo = 0, hi = in.nrows - 1;  // the row holding word t (rows sorted by off)
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (in.rows[mid].off <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const MaskRow row = in.rows[lo];
+    const SceneInfo si = in.scenes[row.scene];
+    const int nwords = (si.n + 31) >> 5;
+    const int64_t local = t - row.off;
+    const int cell = (int)(local / nwords), w = (int)(local % nwords);
+    const float4 ball = in.patch[(int64_t)(si.prim_off + row.emitter) * 16 + (cell & 15)];
+    const float4 ac = in.cone[2 * (cell >> 4)];
+    const float sin_t = in.cone[2 * (cell >> 4) + 1].x;
+    uint32_t bits = 0u;
+    for (int b = 0; b < 32; ++b) {
+        const int j = 32 * w + b;
+        if (j >= si.n) break;
+        const int gj = si.prim_off + j;
+        bool ok = false;
+        for (int k = 0; k < kChainMax && !ok; ++k) {
+            const float4 sph = in.chain[(int64_t)gj * kChainMax + k];
+            if (sph.w < 0.0f) break;
+            ok = cell_reaches(ball, ac, sin_t, sph);
+        }
+        if (ok && plane_separates(ball, ac, sin_t, in.plane[gj])) ok = false;
+        bits |= (ok ? 1u : 0u) << b;
+    }
+    out[t] = bits;
 }
 
 }  // namespace rf

@@ -4,6 +4,7 @@
 // Replaces runCL_GPURNG (RayFactorCL/main.cpp:54-272) and the OpenCL device
 // layer (RayFactorCL/util_opencl.h:133-352) with the CUDA runtime on one GPU.
 #include <algorithm>
+#include <array>
 #include <utility>
 #include <cmath>
 #include <cstdarg>
@@ -38,6 +39,7 @@ struct ApiRange {
 namespace {
 
 constexpr int32_t kMaxPrims = 16384;            // n x n int64 tallies: 2 GiB
+constexpr int64_t kMaskBudgetWords = 1ll << 28;  // cell masks of one upload: at most 1 GiB
 constexpr int64_t kMaxRaysPerEmitter = 1ll << 46;
 
 struct DevBuf {
@@ -115,6 +117,10 @@ struct rf_ctx {
 
     // batched mixed-precision path: scenes concatenated, re-centred in FP64
     DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters;
+    // cell masks of the batched kernel and their inputs (built at upload)
+    DevBuf b_patch, b_chain, b_plane, b_cone, b_maskrows, b_maskoff, b_mask;
+    bool b_masks = false;
+    double b_mask_ms = 0.0;     // device time of the last mask build
     std::vector<SceneInfo> b_info;
     int64_t b_hits_total = 0;
     bool b_single = false;      // b_* hold the scene of rf_set_scene
@@ -397,6 +403,243 @@ float scene_eps(float eps, const float4 *bs, int n)
     return (float)(-(double)eps * std::sqrt(dx * dx + dy * dy + dz * dz));
 }
 
+// --- cell-mask inputs (FP64 on the host, in the scene's re-centred frame) ---
+
+// World point of an object-space point under a re-centred record's m.
+void xf_point(const rf_primitive &e, const double o[3], double w[3])
+{
+    for (int k = 0; k < 3; ++k) {
+        const float *r = e.m + 4 * k;
+        w[k] = (double)r[0] * o[0] + (double)r[1] * o[1] + (double)r[2] * o[2] + (double)r[3];
+    }
+}
+
+// Candidate angles of an angular interval for the extremes of sin and cos:
+// its ends and the multiples of pi/2 inside it.
+int angle_candidates(double t0, double t1, double *out)
+{
+    int k = 0;
+    out[k++] = t0;
+    out[k++] = t1;
+    for (int q = 0; q <= 8; ++q) {
+        const double a = q * (M_PI / 2);
+        if (a > t0 && a < t1) out[k++] = a;
+    }
+    return k;
+}
+
+// Object-space box of parameter patch (pi, pj) of an emitter -- the points its
+// rays start from when r[0] in [pi/4, (pi+1)/4) and r[1] in [pj/4, (pj+1)/4)
+// (emission formulas RayFactorGPU.cl:298-443).  Each coordinate is linear in the
+// radius-like parameter for a fixed angle, and the angle's extremes are at the
+// ends of its interval or at multiples of pi/2, so the listed points bound the
+// patch.  Returns false when the formulas give no finite point (a frustum whose
+// top radius is 1).
+bool patch_box(const rf_primitive &e, int pi, int pj, double lo[3], double hi[3])
+{
+    const double a0 = pi / 4.0, a1 = (pi + 1) / 4.0, b0 = pj / 4.0, b1 = (pj + 1) / 4.0;
+    const double u1 = e.util1, u2 = e.util2;
+    double th[16], pts[64][3];
+    int np = 0, nt;
+    auto add = [&](double x, double y, double z) {
+        pts[np][0] = x; pts[np][1] = y; pts[np][2] = z; ++np;
+    };
+    switch (e.type) {
+    case RF_DISC:
+    case RF_ANNULUS: {
+        double r0, r1;
+        if (e.type == RF_DISC) { r0 = std::sqrt(b0); r1 = std::sqrt(b1); }
+        else {
+            r0 = std::sqrt(std::max(0.0, u1 + (u2 - u1) * b0));
+            r1 = std::sqrt(std::max(0.0, u1 + (u2 - u1) * b1));
+        }
+        nt = angle_candidates(2 * M_PI * a0, 2 * M_PI * a1, th);
+        for (int k = 0; k < nt; ++k)
+            for (double r : {r0, r1}) add(r * std::sin(th[k]), r * std::cos(th[k]), 0.0);
+        break;
+    }
+    case RF_RECTANGLE:
+        for (double x : {2 * a0 - 1, 2 * a1 - 1})
+            for (double y : {2 * b0 - 1, 2 * b1 - 1}) add(x, y, 0.0);
+        break;
+    case RF_CYLINDER:
+        nt = angle_candidates(2 * M_PI * a0, 2 * M_PI * a1, th);
+        for (int k = 0; k < nt; ++k)
+            for (double z : {b0, b1}) add(std::cos(th[k]), std::sin(th[k]), z);
+        break;
+    case RF_FRUSTUM: {
+        auto zf = [&](double a) { return (std::sqrt(1.0 - a + a * u1 * u1) - 1.0) / (u1 - 1.0); };
+        const double z0 = zf(a0), z1 = zf(a1);
+        if (!std::isfinite(z0) || !std::isfinite(z1)) return false;
+        nt = angle_candidates(2 * M_PI * b0, 2 * M_PI * b1, th);
+        for (int k = 0; k < nt; ++k)
+            for (double z : {z0, z1}) {
+                const double rho = 1.0 + z * (u1 - 1.0);
+                add(rho * std::cos(th[k]), rho * std::sin(th[k]), z);
+            }
+        break;
+    }
+    case RF_SPHERE: {
+        double zs[3] = {2 * a0 - 1, 2 * a1 - 1, 0.0};
+        const int nz = (zs[0] < 0.0 && zs[1] > 0.0) ? 3 : 2;
+        nt = angle_candidates(2 * M_PI * b0, 2 * M_PI * b1, th);
+        for (int k = 0; k < nt; ++k)
+            for (int q = 0; q < nz; ++q) {
+                const double rho = std::sqrt(std::max(0.0, 1.0 - zs[q] * zs[q]));
+                add(rho * std::cos(th[k]), rho * std::sin(th[k]), zs[q]);
+            }
+        break;
+    }
+    default:
+        return false;
+    }
+    for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+    for (int q = 0; q < np; ++q)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], pts[q][k]);
+            hi[k] = std::max(hi[k], pts[q][k]);
+        }
+    return true;
+}
+
+// Ball around the image of an object-space box: the image of the box centre and
+// the farthest image of a corner (the image is a parallelepiped), widened for
+// the FP32 emission's rounding and approximations.
+float4 box_ball(const rf_primitive &e, const double lo[3], const double hi[3])
+{
+    const double oc[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+    double c[3], rad = 0.0;
+    xf_point(e, oc, c);
+    for (int q = 0; q < 8; ++q) {
+        const double o[3] = {(q & 1) ? hi[0] : lo[0], (q & 2) ? hi[1] : lo[1], (q & 4) ? hi[2] : lo[2]};
+        double w[3];
+        xf_point(e, o, w);
+        rad = std::max(rad, std::sqrt((w[0] - c[0]) * (w[0] - c[0]) + (w[1] - c[1]) * (w[1] - c[1]) +
+                                      (w[2] - c[2]) * (w[2] - c[2])));
+    }
+    const double cn = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    return make_float4((float)c[0], (float)c[1], (float)c[2], (float)(rad * (1 + 1e-4) + 1e-5 * (cn + rad) + 1e-7));
+}
+
+// Sixteen parameter-patch balls of an emitter (infinite radius when a patch has
+// no finite bound: every surface is then a candidate).
+void patch_balls(const rf_primitive &e, float4 *out)
+{
+    for (int pi = 0; pi < 4; ++pi)
+        for (int pj = 0; pj < 4; ++pj) {
+            double lo[3], hi[3];
+            out[4 * pi + pj] = patch_box(e, pi, pj, lo, hi) ? box_ball(e, lo, hi)
+                                                            : make_float4(0.f, 0.f, 0.f, INFINITY);
+        }
+}
+
+// Spheres covering a surface: for a cylinder or frustum longer than it is wide,
+// a chain of up to kChainMax spheres along its axis (points A + rho(z) (c0 cos +
+// c1 sin) + Z z of slab [z0, z1] lie within rmax * max rho + |Z| (z1 - z0) / 2 of
+// the slab's axis midpoint, rmax the largest radius of the ellipse spanned by the
+// first two columns); otherwise the bounding sphere `bs` (radius in w).
+int surface_chain(const rf_primitive &e, float4 bs, float4 *out)
+{
+    for (int k = 0; k < kChainMax; ++k) out[k] = make_float4(0.f, 0.f, 0.f, -1.f);
+    out[0] = bs;
+    if (e.type != RF_CYLINDER && e.type != RF_FRUSTUM) return 1;
+    double A[3], Z[3], c0[3], c1[3];
+    for (int k = 0; k < 3; ++k) {
+        A[k] = e.m[4 * k + 3];
+        c0[k] = e.m[4 * k + 0];
+        c1[k] = e.m[4 * k + 1];
+        Z[k] = e.m[4 * k + 2];
+    }
+    const double L = std::sqrt(Z[0] * Z[0] + Z[1] * Z[1] + Z[2] * Z[2]);
+    const double g00 = c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2];
+    const double g11 = c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2];
+    const double g01 = c0[0] * c1[0] + c0[1] * c1[1] + c0[2] * c1[2];
+    const double rmax = std::sqrt(0.5 * (g00 + g11 + std::sqrt((g00 - g11) * (g00 - g11) + 4 * g01 * g01)));
+    const double top = e.type == RF_FRUSTUM ? (double)e.util1 : 1.0;
+    const double wide = rmax * std::max(1.0, std::fabs(top));
+    if (!(L > 0.0) || !(wide > 0.0) || !std::isfinite(L + wide)) return 1;
+    const int K = (int)std::min<double>(kChainMax, std::ceil(L / wide));
+    if (K < 2) return 1;
+    for (int k = 0; k < K; ++k) {
+        const double z0 = (double)k / K, z1 = (double)(k + 1) / K, zm = 0.5 * (z0 + z1);
+        const double rho = std::max(std::fabs(1.0 + z0 * (top - 1.0)), std::fabs(1.0 + z1 * (top - 1.0)));
+        const double c[3] = {A[0] + Z[0] * zm, A[1] + Z[1] * zm, A[2] + Z[2] * zm};
+        const double r = rmax * rho + 0.5 * L * (z1 - z0);
+        const double cn = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        out[k] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)(r * (1 + 1e-4) + 1e-5 * (cn + r) + 1e-7));
+    }
+    return K;
+}
+
+// Plane of a disc, annulus or rectangle: object z = 0 is row 2 of invm.
+float4 surface_plane(const rf_primitive &e)
+{
+    if (e.type != RF_DISC && e.type != RF_ANNULUS && e.type != RF_RECTANGLE) return make_float4(0.f, 0.f, 0.f, NAN);
+    const double n[3] = {e.invm[8], e.invm[9], e.invm[10]};
+    const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(nn > 0.0)) return make_float4(0.f, 0.f, 0.f, NAN);
+    return make_float4((float)(n[0] / nn), (float)(n[1] / nn), (float)(n[2] / nn), (float)(-(double)e.invm[11] / nn));
+}
+
+// Unit direction of octahedral-map point (u, v): the inverse of the map that
+// the kernel's direction_cell applies.
+void oct_dir(double u, double v, double d[3])
+{
+    if (std::fabs(u) + std::fabs(v) <= 1.0) {
+        d[0] = u; d[1] = v; d[2] = 1.0 - std::fabs(u) - std::fabs(v);
+    } else {
+        d[0] = (1.0 - std::fabs(v)) * (u < 0 ? -1.0 : 1.0);
+        d[1] = (1.0 - std::fabs(u)) * (v < 0 ? -1.0 : 1.0);
+        d[2] = -(std::fabs(u) + std::fabs(v) - 1.0);
+    }
+    const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    d[0] /= l; d[1] /= l; d[2] /= l;
+}
+
+// Cones of the 256 direction cells, indexed by the kernel's Morton code: axis
+// through the cell's boundary samples, half-angle = the largest angle to a
+// sample (the angle to a fixed axis peaks on the cell's boundary) plus 0.01 rad,
+// far more than the gap between samples (the map moves directions by at most
+// ~2.5 rad per unit of (u, v); samples are 1/2048 apart) and than the kernel's
+// rounding when it assigns a direction to a cell.
+const std::vector<float4> &direction_cones()
+{
+    static std::vector<float4> cones;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cones.assign(512, make_float4(0.f, 0.f, 0.f, 0.f));
+        constexpr int kS = 256;
+        for (int i = 0; i < 16; ++i)
+            for (int j = 0; j < 16; ++j) {
+                const double u0 = -1 + i / 8.0, v0 = -1 + j / 8.0, h = 1 / 8.0;
+                std::vector<std::array<double, 3>> smp;
+                for (int q = 0; q <= kS; ++q) {
+                    const double f = (double)q / kS;
+                    const double uv[4][2] = {{u0 + f * h, v0}, {u0 + f * h, v0 + h}, {u0, v0 + f * h}, {u0 + h, v0 + f * h}};
+                    for (auto &p : uv) {
+                        std::array<double, 3> d;
+                        oct_dir(p[0], p[1], d.data());
+                        smp.push_back(d);
+                    }
+                }
+                double ax[3] = {0, 0, 0};
+                for (auto &d : smp)
+                    for (int k = 0; k < 3; ++k) ax[k] += d[k];
+                const double al = std::sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+                for (int k = 0; k < 3; ++k) ax[k] /= al;
+                double th = 0.0;
+                for (auto &d : smp)
+                    th = std::max(th, std::acos(std::min(1.0, d[0] * ax[0] + d[1] * ax[1] + d[2] * ax[2])));
+                th = std::min(M_PI, th + 0.01);
+                int code = 0;
+                for (int b = 0; b < 4; ++b) code |= (((i >> b) & 1) << (2 * b)) | (((j >> b) & 1) << (2 * b + 1));
+                cones[2 * code] = make_float4((float)ax[0], (float)ax[1], (float)ax[2], (float)std::cos(th));
+                cones[2 * code + 1] = make_float4((float)std::sin(th), 0.f, 0.f, 0.f);
+            }
+    });
+    return cones;
+}
+
 }  // namespace
 
 // Mixed-precision tables of one scene as the batched kernel reads them
@@ -431,7 +674,7 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     if (nprim > (1ll << 31) / 4) return fail(c, RF_ERR_OVERFLOW, "too many surfaces in the batch");
     std::vector<rf_primitive> emit(nprim);
     std::vector<HitRec> tab(nprim);
-    std::vector<float4> bs(nprim);
+    std::vector<float4> bs(nprim), patch((size_t)nprim * 16), chain((size_t)nprim * kChainMax), plane(nprim);
     c->b_info.resize(ns);
     int64_t off = 0, hoff = 0;
     for (int s = 0; s < ns; ++s) {
@@ -439,12 +682,39 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
         prepare_mixed(scenes[s].prims, n, emit.data() + off, tab.data() + off, bs.data() + off);
         c->b_info[s].eps = scene_eps(c->cfg.eps, bs.data() + off, n);
         c->b_info[s].pad = 0;
-        for (int i = 0; i < n; ++i) bs[off + i] = widen_sq(bs[off + i]);
+        for (int i = 0; i < n; ++i) {
+            const int64_t g = off + i;
+            patch_balls(emit[g], patch.data() + g * 16);
+            surface_chain(emit[g], bs[g], chain.data() + g * kChainMax);
+            plane[g] = surface_plane(emit[g]);
+            bs[g] = widen_sq(bs[g]);
+        }
         c->b_info[s].n = n;
         c->b_info[s].prim_off = (int32_t)off;
         c->b_info[s].hits_off = hoff;
         off += n;
         hoff += (int64_t)n * n;
+    }
+    // cell masks for every row of the scenes culling serves (more than
+    // kBatchBruteMax and at most kMaskMaxSurfaces surfaces) while they fit
+    // kMaskBudgetWords
+    std::vector<MaskRow> mrows;
+    std::vector<int64_t> moff(nprim, -1);
+    int64_t mwords = 0;
+    for (int s = 0; s < ns; ++s) {
+        const SceneInfo &si = c->b_info[s];
+        if (si.n <= kBatchBruteMax || si.n > kMaskMaxSurfaces) continue;
+        const int64_t row_words = (int64_t)kMaskCells * ((si.n + 31) / 32);
+        if (mwords + row_words * si.n > kMaskBudgetWords) continue;
+        for (int e = 0; e < si.n; ++e) {
+            MaskRow r;
+            r.scene = s;
+            r.emitter = e;
+            r.off = mwords;
+            mrows.push_back(r);
+            moff[si.prim_off + e] = mwords;
+            mwords += row_words;
+        }
     }
     RF_CUDA(c, cudaSetDevice(c->device));
     RF_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -459,6 +729,40 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     RF_CUDA(c, cudaMemcpyAsync(c->b_emit.p, emit.data(), sizeof(rf_primitive) * nprim, cudaMemcpyHostToDevice, c->stream));
     RF_CUDA(c, cudaMemcpyAsync(c->b_bsph.p, bs.data(), sizeof(float4) * nprim, cudaMemcpyHostToDevice, c->stream));
     RF_CUDA(c, cudaMemcpyAsync(c->b_scenes.p, c->b_info.data(), sizeof(SceneInfo) * ns, cudaMemcpyHostToDevice, c->stream));
+
+    c->b_masks = !mrows.empty();
+    c->b_mask_ms = 0.0;
+    if (c->b_masks) {
+        const std::vector<float4> &cones = direction_cones();
+        RF_CUDA(c, c->b_patch.ensure(sizeof(float4) * patch.size()));
+        RF_CUDA(c, c->b_chain.ensure(sizeof(float4) * chain.size()));
+        RF_CUDA(c, c->b_plane.ensure(sizeof(float4) * plane.size()));
+        RF_CUDA(c, c->b_cone.ensure(sizeof(float4) * cones.size()));
+        RF_CUDA(c, c->b_maskrows.ensure(sizeof(MaskRow) * mrows.size()));
+        RF_CUDA(c, c->b_maskoff.ensure(sizeof(int64_t) * moff.size()));
+        RF_CUDA(c, c->b_mask.ensure(sizeof(uint32_t) * (size_t)mwords));
+        RF_CUDA(c, cudaMemcpyAsync(c->b_patch.p, patch.data(), sizeof(float4) * patch.size(), cudaMemcpyHostToDevice, c->stream));
+        RF_CUDA(c, cudaMemcpyAsync(c->b_chain.p, chain.data(), sizeof(float4) * chain.size(), cudaMemcpyHostToDevice, c->stream));
+        RF_CUDA(c, cudaMemcpyAsync(c->b_plane.p, plane.data(), sizeof(float4) * plane.size(), cudaMemcpyHostToDevice, c->stream));
+        RF_CUDA(c, cudaMemcpyAsync(c->b_cone.p, cones.data(), sizeof(float4) * cones.size(), cudaMemcpyHostToDevice, c->stream));
+        RF_CUDA(c, cudaMemcpyAsync(c->b_maskrows.p, mrows.data(), sizeof(MaskRow) * mrows.size(), cudaMemcpyHostToDevice, c->stream));
+        RF_CUDA(c, cudaMemcpyAsync(c->b_maskoff.p, moff.data(), sizeof(int64_t) * moff.size(), cudaMemcpyHostToDevice, c->stream));
+        MaskInputs in{};
+        in.rows = c->b_maskrows.as<MaskRow>();
+        in.nrows = (int32_t)mrows.size();
+        in.total_words = mwords;
+        in.scenes = c->b_scenes.as<SceneInfo>();
+        in.patch = c->b_patch.as<float4>();
+        in.cone = c->b_cone.as<float4>();
+        in.chain = c->b_chain.as<float4>();
+        in.plane = c->b_plane.as<float4>();
+        RF_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+        RF_CUDA(c, launch_build_masks(in, c->b_mask.as<uint32_t>(), c->stream));
+        RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+        RF_CUDA(c, cudaStreamSynchronize(c->stream));
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->b_mask_ms = ms;
+    }
 
     RF_CUDA(c, cudaStreamSynchronize(c->stream));
     c->b_hits_total = nhits;
@@ -494,6 +798,10 @@ TraceParams batch_params(rf_ctx *c)
     p.key1 = c->cfg.key1;
     p.scene_id = c->cfg.scene_id;
     p.eps = c->cfg.eps;  // per scene: SceneInfo::eps
+    if (c->b_masks) {
+        p.cmask = c->b_mask.as<uint32_t>();
+        p.mask_off = c->b_maskoff.as<int64_t>();
+    }
     return p;
 }
 
@@ -508,7 +816,8 @@ int batched_grid(rf_ctx *c, bool rec)
 {
     int bps = batched_blocks_per_sm(rec, batch_resident(c));
     if (bps <= 0) bps = 1;
-    return c->sms * bps;
+    const int wave = c->sms * bps;
+    return c->cfg.batched_grid > 0 ? std::min(wave, (int)c->cfg.batched_grid) : wave;
 }
 
 // One persistent launch over host-planned segments.
@@ -534,7 +843,7 @@ rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_
     p.rec_base = rec_base;
     const int grid = (int)std::min<int64_t>(batched_grid(c, rec), total_chunks);
     RF_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    RF_CUDA(c, launch_batched(p, rec, batch_resident(c), grid, c->stream));
+    RF_CUDA(c, launch_batched(p, rec, batch_resident(c), c->cfg.work_counts != 0, grid, c->stream));
     RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     c->last_launches = 1;
     c->timed = true;
@@ -599,6 +908,7 @@ rf_status rf_create(rf_ctx **out, const rf_config *cfg)
         return RF_ERR_INVALID_ARG;
     if (c.block_size < 0 || c.block_size > kBlock || (c.block_size % 32) != 0) return RF_ERR_INVALID_ARG;
     if (c.tally_mode < 0 || c.tally_mode > 2 || c.table_mode < 0 || c.table_mode > 2) return RF_ERR_INVALID_ARG;
+    if (c.work_counts < 0 || c.work_counts > 1 || c.batched_grid < 0) return RF_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
         cudaGetLastError();
@@ -633,7 +943,8 @@ void rf_destroy(rf_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (DevBuf *b : {&c->d_tab, &c->d_emit, &c->d_bvtab, &c->d_bvinfo, &c->d_hits, &c->d_seg,
                       &c->d_rays, &c->d_F, &c->d_rec, &c->d_err, &c->d_misc, &c->b_tab, &c->b_emit,
-                      &c->b_bsph, &c->b_scenes, &c->b_hits, &c->b_rows, &c->b_counters})
+                      &c->b_bsph, &c->b_scenes, &c->b_hits, &c->b_rows, &c->b_counters, &c->b_patch,
+                      &c->b_chain, &c->b_plane, &c->b_cone, &c->b_maskrows, &c->b_maskoff, &c->b_mask})
         b->release();
     c->h_seg.release();
     c->h_rays.release();
@@ -1253,7 +1564,8 @@ rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_sc
         cudaError_t e;
         if ((e = launch_plan_round(nrows, d_sc, d_em, d_total, d_next, c->d_seg.as<Segment>(), &bc->nseg, &bc->total, &bc->queue,
                                    kBatchChunkDraws, c->stream)) != cudaSuccess) return e;
-        if ((e = launch_batched(p, false, batch_resident(c), grid, c->stream)) != cudaSuccess) return e;
+        if ((e = launch_batched(p, false, batch_resident(c), c->cfg.work_counts != 0, grid, c->stream)) != cudaSuccess)
+            return e;
         if ((e = launch_converge_step(c->b_hits.as<unsigned long long>(), d_total, d_off, d_len, nrows, nullptr,
                                       tol, d_next, round_rays, &bc->flags[0], c->stream)) != cudaSuccess) return e;
         return launch_decide_round(&bc->flags[0], max_rounds, h, c->stream);

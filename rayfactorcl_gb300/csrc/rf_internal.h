@@ -63,7 +63,32 @@ struct TraceParams {
     const int64_t *d_total;         // batched kernel: device-resident chunk count (or null)
     const int32_t *d_nseg;          // batched kernel: device-resident segment count (or null)
     unsigned long long *work;       // batched kernel: [0..5] ray x surface tests by type,
-                                    // [6] packet x surface cone tests, [7] packets
+                                    // [6] candidate surfaces of packets, [7] packets
+    const uint32_t *cmask;          // batched kernel: cell masks of all rows that have them
+    const int64_t *mask_off;        // per global row (prim_off + emitter): first mask word, -1 = none
+};
+
+// Cell masks of the batched kernel (build_masks_kernel): one bit per surface for
+// each of kMaskCells sort keys of a row (scene, emitter).
+constexpr int kMaskCells = 4096;
+constexpr int kChainMax = 8;            // bounding spheres per surface in the mask test
+constexpr int kMaskMaxSurfaces = 1024;  // scenes up to this many surfaces get masks
+
+struct MaskRow {
+    int32_t scene;
+    int32_t emitter;
+    int64_t off;     // first word of the row's masks (kMaskCells x ceil(n/32) words)
+};
+
+struct MaskInputs {
+    const MaskRow *rows;      // sorted by off
+    int32_t nrows;
+    int64_t total_words;
+    const SceneInfo *scenes;
+    const float4 *patch;      // per global prim: 16 parameter-patch balls (centre, radius)
+    const float4 *cone;       // 256 direction cells: (axis, cos theta), (sin theta, 0, 0, 0)
+    const float4 *chain;      // per global prim: kChainMax spheres (centre, radius; radius < 0: none)
+    const float4 *plane;      // per global prim: (unit normal, normal . point); w NaN: not planar
 };
 
 constexpr int kBlock = 256;    // maximum threads per block of the single-scene kernels
@@ -89,12 +114,15 @@ struct LaunchCfg {
 template <class M> cudaError_t launch_trace(const LaunchCfg &cfg, const TraceParams &p, cudaStream_t st);
 template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
 
-// Batched mixed-precision persistent kernel (rf_kern_fast.cu).
-cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, int grid, cudaStream_t st);
+// Batched mixed-precision persistent kernel (rf_kern_fast.cu); count: also
+// collect the work counters (TraceParams::work).
+cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool count, int grid, cudaStream_t st);
 int batched_blocks_per_sm(bool rec, bool resident);
+cudaError_t launch_build_masks(const MaskInputs &in, uint32_t *out, cudaStream_t st);
 size_t batched_smem_bytes();
 int batched_tile();  // scenes with at most this many surfaces use the resident kernel
 constexpr int kBatchTile = 512;  // surfaces the resident kernel keeps in shared memory
+constexpr int kBatchBruteMax = 12;  // scenes up to this many surfaces are traced without culling
 constexpr int kBatchMaxSurfaces = 32767;  // nearest hits are kept as int16 in shared memory
 constexpr int kBatchChunkDraws = 8192;  // Philox draws per chunk of the batched kernel
 

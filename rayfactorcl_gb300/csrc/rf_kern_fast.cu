@@ -12,20 +12,22 @@ static_assert(kBatchThreads * kBatchDraws == kBatchChunkDraws, "chunk size");
 
 size_t batched_smem_bytes() { return sizeof(BatchSmem); }
 
-template <bool REC, bool RES>
+template <bool REC, bool RES, bool CNT>
 static cudaError_t launch_b(const TraceParams &p, int grid, cudaStream_t st)
 {
     const size_t smem = sizeof(BatchSmem);
-    cudaError_t e = cudaFuncSetAttribute(batched_kernel<REC, RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto k = batched_kernel<REC, RES, CNT>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    batched_kernel<REC, RES><<<grid, kBatchThreads, smem, st>>>(p);
+    k<<<grid, kBatchThreads, smem, st>>>(p);
     return cudaGetLastError();
 }
 
-cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, int grid, cudaStream_t st)
+cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool count, int grid, cudaStream_t st)
 {
-    if (rec) return resident ? launch_b<true, true>(p, grid, st) : launch_b<true, false>(p, grid, st);
-    return resident ? launch_b<false, true>(p, grid, st) : launch_b<false, false>(p, grid, st);
+    if (rec) return resident ? launch_b<true, true, false>(p, grid, st) : launch_b<true, false, false>(p, grid, st);
+    if (count) return resident ? launch_b<false, true, true>(p, grid, st) : launch_b<false, false, true>(p, grid, st);
+    return resident ? launch_b<false, true, false>(p, grid, st) : launch_b<false, false, false>(p, grid, st);
 }
 
 template <bool REC, bool RES>
@@ -33,8 +35,9 @@ static int occ_b()
 {
     const size_t smem = sizeof(BatchSmem);
     int nb = 0;
-    cudaFuncSetAttribute(batched_kernel<REC, RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<REC, RES>, kBatchThreads, smem);
+    auto k = batched_kernel<REC, RES, false>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kBatchThreads, smem);
     return nb;
 }
 
@@ -42,6 +45,15 @@ int batched_blocks_per_sm(bool rec, bool resident)
 {
     if (rec) return resident ? occ_b<true, true>() : occ_b<true, false>();
     return resident ? occ_b<false, true>() : occ_b<false, false>();
+}
+
+cudaError_t launch_build_masks(const MaskInputs &in, uint32_t *out, cudaStream_t st)
+{
+    if (in.total_words <= 0) return cudaSuccess;
+    const int64_t blocks = (in.total_words + 255) / 256;
+    if (blocks > 0x7fffffff) return cudaErrorInvalidValue;
+    build_masks_kernel<<<(unsigned)blocks, 256, 0, st>>>(in, out);
+    return cudaGetLastError();
 }
 
 int batched_tile() { return kBatchTile; }

@@ -155,5 +155,5 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     int bps = batched_blocks_per_sm(false, true);
     if (bps <= 0) bps = 1;
     const int grid = (int)(chunks < (int64_t)sms * bps ? chunks : (int64_t)sms * bps);
-    return launch_batched(p, false, true, grid, st) == cudaSuccess ? RF_OK : RF_ERR_CUDA;
+    return launch_batched(p, false, true, false, grid, st) == cudaSuccess ? RF_OK : RF_ERR_CUDA;
 }

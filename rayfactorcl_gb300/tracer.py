@@ -28,7 +28,8 @@ class Tracer:
 
     def __init__(self, precision: int = PREC_EXACT, compat: int = 0, key1: int = REF_KEY1,
                  eps: float = 1e-3, device: int = 0, block_size: int = 0, rays_per_thread: int = 0,
-                 scene_id: int = 0, tally_mode: int = 0, table_mode: int = 0, test_order: int = 0):
+                 scene_id: int = 0, tally_mode: int = 0, table_mode: int = 0, test_order: int = 0,
+                 work_counts: bool = False, batched_grid: int = 0):
         L = _lib.load()
         cfg = _lib.RfConfig()
         L.rf_config_default(ctypes.byref(cfg))
@@ -43,6 +44,8 @@ class Tracer:
         cfg.tally_mode = tally_mode
         cfg.table_mode = table_mode
         cfg.test_order = test_order
+        cfg.work_counts = 1 if work_counts else 0
+        cfg.batched_grid = batched_grid
         h = ctypes.c_void_p()
         check(L.rf_create(ctypes.byref(h), ctypes.byref(cfg)))
         self._h = h

@@ -283,3 +283,26 @@ def test_mixed_far_offset_self_hits(built_lib, oracle_lib):
         h64, _ = t.trace(rays)
     for e in range(4):
         assert hm[e, e] == 0 and h64[e, e] == 0
+
+
+@pytest.mark.parametrize("name", ["gen_mixed64", "gen_furnace", "gen_sweep0"])
+def test_mixed_results_independent_of_scheduling(built_lib, name):
+    """A ray's result depends on the ray alone: the same budgets traced with
+    different persistent grids (so chunks meet different blocks and packets form in
+    a different order), with and without the work counters, give identical tallies;
+    so do two runs in a row."""
+    sc = golden_scene(name)
+    rng = np.random.default_rng(3)
+    rays = (rng.integers(1, 40000, sc.n) * 4 + rng.integers(0, 4, sc.n)).astype(np.int64)
+    runs = []
+    for grid, count in ((0, False), (0, False), (7, False), (61, True), (1, False)):
+        with _tracer(sc, precision=PREC_MIXED, batched_grid=grid, work_counts=count) as t:
+            hits, _ = t.trace(rays)
+            runs.append(hits)
+            w = t.work_counts()
+            if count:
+                assert int(w[:6].sum()) > 0 and int(w[7]) > 0 and int(w[6]) >= int(w[:6].sum()) // 32
+            else:
+                assert int(w.sum()) == 0
+    for h in runs[1:]:
+        assert np.array_equal(h, runs[0])
