@@ -20,8 +20,8 @@
 //      parameter patch can reach), or, for scenes without masks, the surfaces
 //      whose bounding sphere the packet's origin ball and direction cone can
 //      reach.  For each candidate (in index order) every lane checks its own ray
-//      against the surface's bounding sphere and its own cell's mask bit, and
-//      the full test runs only if some lane passes,
+//      against the surface's bounding sphere, and the full test runs only if
+//      some lane passes,
 //   4. evaluates the surviving tests in FP32, with quadric discriminants in
 //      cancellation-free forms; a discriminant within 16 rounding errors of
 //      its terms (a grazing ray), or a cone whose A lost 12 bits, is
@@ -29,13 +29,13 @@
 //   5. tallies first hits in a shared-memory row histogram (flushed as 64-bit
 //      atomics whenever the (scene, emitter) row changes) straight from the
 //      packet loop.
-// A lane keeps a test's result only when its own checks passed (step 3), so a
-// ray's result depends on the ray alone, never on the rays it shares a packet
-// with: the per-lane gate is a function of the ray (its cell mask bit and its
-// sphere check), and every surface that passes it is tested because its mask
-// bit puts it among the packet's candidates.  Skipping a surface that the
-// ray cannot reach does not change its nearest hit; only the arithmetic
-// differs from the exact kernel.  Scenes of at most kBruteMax surfaces skip
+// A ray's result depends on the ray alone, never on the rays it shares a packet
+// with: it is the nearest hit among the surfaces the ray's own gate admits (its
+// cell mask bit and its sphere check, both functions of the ray), every one of
+// which its packet tests; a lane whose packet-wide winner fails its own gate,
+// or that deferred more than one test, re-traces over its gated set.  Skipping
+// a surface that the ray cannot reach does not change its nearest hit; only the
+// arithmetic differs from the exact kernel.  Scenes of at most kBruteMax surfaces skip
 // steps 1-3: every thread tests its own rays against all surfaces.
 #pragma once
 
@@ -665,14 +665,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
 #pragma unroll 1
                     for (int w = 0; w < nwords; ++w) {
                         const int jw = j0 + (w << 5);
-                        unsigned mine, cm;
-                        if (mcell) {  // block-uniform
-                            mine = __ldg(mcell + (jw >> 5));
-                            cm = __reduce_or_sync(0xffffffffu, mine);
-                        } else {
-                            mine = 0xffffffffu;
-                            cm = __shfl_sync(0xffffffffu, cmask, w);
-                        }
+                        const unsigned cm0 = mcell ? __reduce_or_sync(0xffffffffu, __ldg(mcell + (jw >> 5)))
+                                                   : __shfl_sync(0xffffffffu, cmask, w);  // block-uniform choice
+                        unsigned cm = cm0;
                         if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
                         // two candidates per pass: their sphere checks are independent
                         // chains (latency hidden); tests still run in index order
@@ -684,36 +679,45 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             const int ja = jw + ba_, jb = jw + (bb_ >= 0 ? bb_ : ba_);
                             const float4 sa = resident ? S.bs[ja] : __ldg(gbs + ja);
                             const float4 sb = resident ? S.bs[jb] : __ldg(gbs + jb);
-                            const bool ma = ((mine >> ba_) & 1u) && ray_may_hit(ray, idd, sa);
-                            const bool mb = bb_ >= 0 && ((mine >> bb_) & 1u) && ray_may_hit(ray, idd, sb);
+                            const bool ma = ray_may_hit(ray, idd, sa);
+                            const bool mb = bb_ >= 0 && ray_may_hit(ray, idd, sb);
                             const unsigned va = __ballot_sync(0xffffffffu, ma);
                             const unsigned vb = __ballot_sync(0xffffffffu, mb);
 #pragma unroll
                             for (int q = 0; q < 2; ++q) {
                                 if (!(q ? vb : va)) continue;  // warp-uniform
                                 const int j = q ? jb : ja;
-                                const bool gate = q ? mb : ma;
                                 const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
                                 const int type = __float_as_int(h.aux.x);
                                 if (COUNT) tcount += lane == type ? nvalid : 0;
                                 bool defer = false;
                                 const float t = hit_mixed(type, h, ray, eps, sc, defer);
-                                if (gate && t < tb) { tb = t; bi = j; }
-                                const bool dg = gate && defer;
-                                ndef += dg;  // predicated, no branch
-                                dj = dg ? j : dj;
+                                if (t < tb) { tb = t; bi = j; }
+                                ndef += defer;  // predicated, no branch
+                                dj = defer ? j : dj;
                             }
                         }
                     }
                 }
-                // the deferred test in FP64 (lower index wins a tie: it ran out of order);
-                // a lane that deferred more than one test re-traces its ray (cold)
+                // The lane's result must be its nearest hit among the surfaces its own
+                // gate admits (the set its cell mask and sphere check select), which
+                // depends on the ray alone.  The loop above took the nearest over the
+                // packet's tested surfaces, a superset; when the winner passes the
+                // lane's gate it is also the nearest of the gated set (same index-order
+                // ties), otherwise -- or when the lane deferred more than one test --
+                // the lane re-traces over its gated set (cold).  A single deferred test
+                // is re-evaluated in FP64 (lower index wins a tie: it ran out of order).
+                bool retrace = valid && ndef > 1;
                 if (valid && ndef == 1) {
                     const HitRec hq = RESIDENT ? S.tab[dj] : load_rec(gtab, dj);
                     const float t = hit_f64(hq, ray, eps, sc);
                     if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
                     ++nref;
-                } else if (valid && ndef > 1) {
+                    retrace = !own_gate(mcell, dj, ray, idd, resident ? S.bs[dj] : __ldg(gbs + dj));
+                }
+                if (valid && !retrace && bi >= 0)
+                    retrace = !own_gate(mcell, bi, ray, idd, resident ? S.bs[bi] : __ldg(gbs + bi));
+                if (retrace) {
                     bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc);
                     nref += 2;
                 }
