@@ -271,10 +271,10 @@ def run_ours(args):
     # -- headline kernel: scene resident, per-step device time ------------
     t, stream = tracer(headline)
     head_bv = plain_bv and headline != PREC_MIXED
-    if headline != PREC_MIXED:
-        t.trace_async(rays, head_bv)
-        t.read_results(None, None)
-        t.autotune(head_bv)
+    # launch shape (plain kernels) or kernel choice (mixed: small-scene vs batched) for these budgets
+    t.trace_async(rays, head_bv)
+    t.read_results(None, None)
+    t.autotune(head_bv)
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:

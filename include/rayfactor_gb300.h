@@ -315,7 +315,7 @@ rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s);
  * on it and must be serialised by the caller.
  * ------------------------------------------------------------------------- */
 #define RF_NOALLOC_MAX_PRIMS 512
-#define RF_NOALLOC_SCRATCH_BYTES (120 * 1024)
+#define RF_NOALLOC_SCRATCH_BYTES (160 * 1024)
 
 rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n_prims,
                                  const int64_t *rays_per_emitter, uint32_t compat, uint32_t key1,

@@ -57,6 +57,7 @@ constexpr float kCondA = 1.0f / 4096.0f;                         // 12 bits lost
 static_assert(kCells == 4 * kBatchThreads, "the bucket scan gives each thread four buckets");
 static_assert(kCells == kMaskCells, "one mask per sort key");
 static_assert(kChunkRays <= 65536, "ray indices of a chunk are 16-bit");
+constexpr int kFrameWords = kEmitFrameWords;                     // float4 words of an EmitFrame
 
 // Rays are not stored: the lane that traces a ray re-emits it from its draw's
 // uniforms, kept as 4 x 24 bits in three words (u01 uses only the top 24 bits of
@@ -72,6 +73,7 @@ struct BatchSmem {
     float4 bs[kBatchTile];              // bounding spheres, squared widened radius in w
     int hist[kBatchHist];
     rf_primitive emit;
+    float4 frame[kFrameWords];
     int64_t chunk;
     int next_packet;
     int n_valid;
@@ -99,6 +101,39 @@ __device__ __forceinline__ void unpack_uniforms(uint32_t w0, uint32_t w1, uint32
     uf[1] = __fmul_rn(__uint2float_rn(b), 0x1p-24f);
     uf[2] = __fmul_rn(__uint2float_rn(c), 0x1p-24f);
     uf[3] = __fmul_rn(__uint2float_rn(d), 0x1p-24f);
+}
+
+// Emission of the mixed-precision kernels.  A planar emitter (disc, annulus,
+// rectangle) has one world frame for all its rays: EmitFrame holds its origin
+// and in-plane axes (the columns of m) and the rotation that alignRayDirection
+// (RayFactorGPU.cl:87-97) applies to its fixed normal, all computed on the host
+// in FP64 (with the FP64 tracer's cancellation-free 1 + n.z for a normal facing
+// -z), so a ray costs the point's sin/cos and square root, the local direction
+// and 15 multiply-adds.  Curved emitters keep the per-ray normal of emit_ray.
+// frame[0] = (origin, planar flag), frame[1] = (x axis, R22), frame[2] = (y
+// axis, 0), frame[3] = (R00, R01, R02, R10), frame[4] = (R11, R12, R20, R21).
+__device__ __forceinline__ Ray<float> emit_mixed(const rf_primitive &e, const float4 *f, const float r[4])
+{
+    if (f[0].w == 0.0f) return emit_ray<MFast>(e, r);  // the same for every ray of the emitter
+    float px, py, sn, cs, t;
+    if (e.type == RF_RECTANGLE) {  // RayFactorGPU.cl:399-417
+        px = 2.0f * r[0] - 1.0f;
+        py = 2.0f * r[1] - 1.0f;
+    } else {  // disc RayFactorGPU.cl:298-321, annulus :323-345
+        MFast::sincos(r[0] * k2PiF, sn, cs);
+        t = e.type == RF_DISC ? MFast::sqrt(r[1]) : MFast::sqrt((e.util2 - e.util1) * r[1] + e.util1);
+        px = t * sn;
+        py = t * cs;
+    }
+    const V3<float> o = os_ray_direction<MFast>(r);
+    Ray<float> ray;
+    ray.sx = fmaf(px, f[1].x, fmaf(py, f[2].x, f[0].x));
+    ray.sy = fmaf(px, f[1].y, fmaf(py, f[2].y, f[0].y));
+    ray.sz = fmaf(px, f[1].z, fmaf(py, f[2].z, f[0].z));
+    ray.cx = fmaf(f[3].x, o.x, fmaf(f[3].y, o.y, f[3].z * o.z));
+    ray.cy = fmaf(f[3].w, o.x, fmaf(f[4].x, o.y, f[4].y * o.z));
+    ray.cz = fmaf(f[4].z, o.x, fmaf(f[4].w, o.y, f[1].w * o.z));
+    return ray;
 }
 
 // Octahedral cell of a direction, kDirGrid x kDirGrid cells in Morton order.
@@ -340,6 +375,16 @@ __device__ __forceinline__ int ray_key(const Ray<float> &ray, const float r[4])
            min(3, (int)(r[1] * 4.0f));
 }
 
+// A planar emitter (disc, annulus, rectangle) cannot be hit by its own rays:
+// they leave its plane into the open half-space of its normal (o.z =
+// sqrt(1 - r[3]) >= 2^-12, RayFactorGPU.cl:115), so t = 0 is the only
+// intersection; an FP32 "self-hit" further on is rounding (the FP64 tracer has
+// none).  The mixed kernels skip that test; -1 = nothing to skip.
+__device__ __forceinline__ int self_skip(const rf_primitive &e, int emitter)
+{
+    return (e.type == RF_DISC || e.type == RF_ANNULUS || e.type == RF_RECTANGLE) ? emitter : -1;
+}
+
 // The lane's own gate for surface j: its cell's mask bit (when the scene has
 // masks) and its ray's bounding-sphere check.
 __device__ __forceinline__ bool own_gate(const uint32_t *mcell, int j, const Ray<float> &ray, float idd,
@@ -354,17 +399,39 @@ __device__ __forceinline__ bool own_gate(const uint32_t *mcell, int j, const Ray
 // one test, and a lane keeps only one).
 __device__ __noinline__ int retrace_f64(int n, bool resident, const HitRec *stab, const HitRec *gtab,
                                         const float4 *sbs, const float4 *gbs, const uint32_t *mcell,
-                                        const Ray<float> &ray, float idd, float eps, bool sc)
+                                        const Ray<float> &ray, float idd, float eps, bool sc, int skip)
 {
     float tb = MFast::inf();
     int bi = -1;
     for (int j = 0; j < n; ++j) {
-        if (!own_gate(mcell, j, ray, idd, resident ? sbs[j] : __ldg(gbs + j))) continue;
+        if (j == skip || !own_gate(mcell, j, ray, idd, resident ? sbs[j] : __ldg(gbs + j))) continue;
         const HitRec h = resident ? stab[j] : load_rec(gtab, j);
         bool defer = false;
         float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
         if (defer) t = hit_f64(h, ray, eps, sc);
         if (t < tb) { tb = t; bi = j; }
+    }
+    return bi;
+}
+
+// Nearest hit of a ray tested against all n surfaces: bi / tb from the index-order
+// loop, dj the deferred test (-1 none, j the only one, -2 several).  One deferral
+// is re-evaluated in FP64 (lower index wins a tie: it ran out of order); several
+// re-trace the ray with FP64 for each.  Shared by the small-scene paths of the
+// batched kernel and of mixed_small_kernel, so both give the same result.
+__device__ __forceinline__ int resolve_brute(int bi, float tb, int dj, int n, bool resident, const HitRec *stab,
+                                             const HitRec *gtab, const float4 *sbs, const float4 *gbs,
+                                             const Ray<float> &ray, float eps, bool sc, int skip, int &nref)
+{
+    if (dj >= 0) {
+        const HitRec hq = resident ? stab[dj] : load_rec(gtab, dj);
+        const float t = hit_f64(hq, ray, eps, sc);
+        if (t < tb || (t == tb && bi >= 0 && dj < bi)) bi = dj;
+        ++nref;
+    } else if (dj == -2) {
+        bi = retrace_f64(n, resident, stab, gtab, sbs, gbs, nullptr, ray,
+                         MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz), eps, sc, skip);
+        nref += 2;
     }
     return bi;
 }
@@ -455,6 +522,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
             if (tid < (int)(sizeof(rf_primitive) / 4))
                 reinterpret_cast<float *>(&S.emit)[tid] =
                     reinterpret_cast<const float *>(p.emit + si.prim_off + sg.emitter)[tid];
+            if (tid < kFrameWords) S.frame[tid] = p.frame[(int64_t)(si.prim_off + sg.emitter) * kFrameWords + tid];
             cur_emitter = sg.emitter;
             mrow = nullptr;
             if (p.mask_off) {
@@ -469,6 +537,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
         const uint32_t sid = (p.compat & RF_COMPAT_STREAMS) ? 0u : (p.scene_id + (uint32_t)sg.scene);
         const HitRec *gtab = p.tab + si.prim_off;
         unsigned long long *grow = p.hits + si.hits_off + (int64_t)cur_emitter * si.n;
+        const int skip = self_skip(S.emit, cur_emitter);  // block-uniform
 
         if (si.n <= kBruteMax) {  // block-uniform: too few surfaces for culling to pay
             // every thread traces its own rays against all surfaces in index order
@@ -489,27 +558,20 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         float r[4];
 #pragma unroll
                         for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
-                        const Ray<float> ray = emit_ray<MFast>(S.emit, r);
+                        const Ray<float> ray = emit_mixed(S.emit, S.frame, r);
                         float tb = MFast::inf();
                         int dj = -1;
 #pragma unroll 1
                         for (int j = 0; j < si.n; ++j) {
+                            if (j == skip) continue;  // uniform: every thread's emitter
                             const HitRec h = RESIDENT ? S.tab[j] : load_rec(gtab, j);
                             bool defer = false;
                             const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
                             if (t < tb) { tb = t; bi = j; }
                             dj = defer ? (dj == -1 ? j : -2) : dj;
                         }
-                        if (dj >= 0) {
-                            const HitRec hq = RESIDENT ? S.tab[dj] : load_rec(gtab, dj);
-                            const float t = hit_f64(hq, ray, eps, sc);
-                            if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
-                            ++nref;
-                        } else if (dj == -2) {
-                            bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, S.bs, p.bsph + si.prim_off, nullptr, ray,
-                                             MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz), eps, sc);
-                            nref += 2;
-                        }
+                        bi = resolve_brute(bi, tb, dj, si.n, RESIDENT, S.tab, gtab, S.bs, p.bsph + si.prim_off,
+                                           ray, eps, sc, skip, nref);
                     }
                     // all 32 lanes reach the warp-wide calls below
                     if (COUNT) nv_warp += __popc(__ballot_sync(0xffffffffu, valid));
@@ -551,7 +613,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     float r[4];
 #pragma unroll
                     for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
-                    const Ray<float> ray = emit_ray<MFast>(S.emit, r);  // the origin is dead code here
+                    const Ray<float> ray = emit_mixed(S.emit, S.frame, r);  // the origin is dead code here
                     const int64_t rid = gid * 4 + v;
                     const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
                     key4[v] = valid ? ray_key(ray, r) : kCells;
@@ -640,7 +702,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     const int q = (i + v + 1) & 3;
                     r[i] = q == 0 ? uf[0] : (q == 1 ? uf[1] : (q == 2 ? uf[2] : uf[3]));
                 }
-                const Ray<float> ray = emit_ray<MFast>(S.emit, r);
+                const Ray<float> ray = emit_mixed(S.emit, S.frame, r);
                 const float idd = MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
                 const uint32_t *mcell = mrow ? mrow + (int64_t)ray_key(ray, r) * nwords_all : nullptr;
                 float tb = MFast::inf();
@@ -667,7 +729,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         const int jw = j0 + (w << 5);
                         const unsigned cm0 = mcell ? __reduce_or_sync(0xffffffffu, __ldg(mcell + (jw >> 5)))
                                                    : __shfl_sync(0xffffffffu, cmask, w);  // block-uniform choice
-                        unsigned cm = cm0;
+                        unsigned cm = cm0 & ~((skip >= jw && skip < jw + 32) ? (1u << (skip - jw)) : 0u);
                         if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
                         // two candidates per pass: their sphere checks are independent
                         // chains (latency hidden); tests still run in index order
@@ -718,7 +780,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 if (valid && !retrace && bi >= 0)
                     retrace = !own_gate(mcell, bi, ray, idd, resident ? S.bs[bi] : __ldg(gbs + bi));
                 if (retrace) {
-                    bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc);
+                    bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc, skip);
                     nref += 2;
                 }
                 if (REC && valid) p.rec[gid0 * 4 + l - p.rec_base] = bi;

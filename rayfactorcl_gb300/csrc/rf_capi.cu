@@ -118,7 +118,7 @@ struct rf_ctx {
     // batched mixed-precision path: scenes concatenated, re-centred in FP64
     DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters;
     // cell masks of the batched kernel and their inputs (built at upload)
-    DevBuf b_patch, b_chain, b_plane, b_cone, b_maskrows, b_maskoff, b_mask;
+    DevBuf b_patch, b_chain, b_plane, b_cone, b_maskrows, b_maskoff, b_mask, b_frame;
     bool b_masks = false;
     double b_mask_ms = 0.0;     // device time of the last mask build
     std::vector<SceneInfo> b_info;
@@ -126,6 +126,11 @@ struct rf_ctx {
     bool b_single = false;      // b_* hold the scene of rf_set_scene
     unsigned long long last_refined = 0;
     unsigned long long last_work[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // single-scene MIXED traces: 0 = by surface count, 1 = small-scene kernel,
+    // 2 = batched kernel (set by rf_autotune)
+    int mixed_path = 0;
+    bool last_small = false;                 // the last MIXED launch was the small-scene kernel
+    unsigned long long small_work[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -642,6 +647,31 @@ const std::vector<float4> &direction_cones()
 
 }  // namespace
 
+// Planar emitters: origin and in-plane axes (columns of m), and the rotation of
+// alignRayDirection (RayFactorGPU.cl:87-97) for the fixed normal n = row 2 of invm,
+// normalised (transformNormal of (0,0,1), :73-85), all in FP64.  d = 1/(1 + n.z),
+// formed as (1 - n.z)/(n.x^2 + n.y^2) for a normal facing -z (the same value for
+// a unit normal, without cancellation), and 0.5 where it is infinite (:91).
+void rf::emit_frame(const rf_primitive &e, float4 *f)
+{
+    for (int k = 0; k < kEmitFrameWords; ++k) f[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (e.type != RF_DISC && e.type != RF_ANNULUS && e.type != RF_RECTANGLE) return;  // flag 0: per-ray normal
+    double n[3] = {e.invm[8], e.invm[9], e.invm[10]};
+    const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(nn > 0.0) || !std::isfinite(nn)) return;
+    for (double &v : n) v /= nn;
+    double d = n[2] < 0.0 ? (1.0 - n[2]) / (n[0] * n[0] + n[1] * n[1]) : 1.0 / (1.0 + n[2]);
+    if (std::isinf(d)) d = 0.5;
+    const double R[9] = {n[2] + d * n[1] * n[1], -d * n[0] * n[1], n[0],
+                         -d * n[0] * n[1], n[2] + d * n[0] * n[0], n[1],
+                         -n[0], -n[1], n[2]};
+    f[0] = make_float4(e.m[3], e.m[7], e.m[11], 1.0f);
+    f[1] = make_float4(e.m[0], e.m[4], e.m[8], (float)R[8]);
+    f[2] = make_float4(e.m[1], e.m[5], e.m[9], 0.0f);
+    f[3] = make_float4((float)R[0], (float)R[1], (float)R[2], (float)R[3]);
+    f[4] = make_float4((float)R[4], (float)R[5], (float)R[6], (float)R[7]);
+}
+
 // Mixed-precision tables of one scene as the batched kernel reads them
 // (re-centred transforms, hit records, bounding spheres with squared radius)
 // and the scene's self-hit threshold (eps < 0: relative, as rf_trace forms it).
@@ -674,7 +704,8 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     if (nprim > (1ll << 31) / 4) return fail(c, RF_ERR_OVERFLOW, "too many surfaces in the batch");
     std::vector<rf_primitive> emit(nprim);
     std::vector<HitRec> tab(nprim);
-    std::vector<float4> bs(nprim), patch((size_t)nprim * 16), chain((size_t)nprim * kChainMax), plane(nprim);
+    std::vector<float4> bs(nprim), patch((size_t)nprim * 16), chain((size_t)nprim * kChainMax), plane(nprim),
+        frame((size_t)nprim * kEmitFrameWords);
     c->b_info.resize(ns);
     int64_t off = 0, hoff = 0;
     for (int s = 0; s < ns; ++s) {
@@ -687,6 +718,7 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
             patch_balls(emit[g], patch.data() + g * 16);
             surface_chain(emit[g], bs[g], chain.data() + g * kChainMax);
             plane[g] = surface_plane(emit[g]);
+            emit_frame(emit[g], frame.data() + g * kEmitFrameWords);
             bs[g] = widen_sq(bs[g]);
         }
         c->b_info[s].n = n;
@@ -722,6 +754,9 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     RF_CUDA(c, c->b_emit.ensure(sizeof(rf_primitive) * nprim));
     RF_CUDA(c, c->b_bsph.ensure(sizeof(float4) * nprim));
     RF_CUDA(c, c->b_scenes.ensure(sizeof(SceneInfo) * ns));
+    RF_CUDA(c, c->b_frame.ensure(sizeof(float4) * frame.size()));
+    RF_CUDA(c, cudaMemcpyAsync(c->b_frame.p, frame.data(), sizeof(float4) * frame.size(), cudaMemcpyHostToDevice,
+                               c->stream));
 
     RF_CUDA(c, c->b_hits.ensure((size_t)nhits * 8));
     RF_CUDA(c, c->b_counters.ensure(256));
@@ -787,6 +822,7 @@ TraceParams batch_params(rf_ctx *c)
     p.tab = c->b_tab.as<HitRec>();
     p.emit = c->b_emit.as<rf_primitive>();
     p.bsph = c->b_bsph.as<float4>();
+    p.frame = c->b_frame.as<float4>();
     p.scenes = c->b_scenes.as<SceneInfo>();
 
     p.hits = c->b_hits.as<unsigned long long>();
@@ -824,6 +860,7 @@ int batched_grid(rf_ctx *c, bool rec)
 rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_chunks, bool rec,
                       int32_t *d_rec, int64_t rec_base, bool zero_hits)
 {
+    c->last_small = false;
     c->last_launches = 0;
     c->timed = false;
     if (zero_hits) RF_CUDA(c, cudaMemsetAsync(c->b_hits.p, 0, (size_t)c->b_hits_total * 8, c->stream));
@@ -848,6 +885,83 @@ rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_
     c->last_launches = 1;
     c->timed = true;
     return RF_OK;
+}
+
+// Single scenes of at most this many surfaces take the small-scene kernel
+// unless rf_autotune measured otherwise.
+constexpr int kSmallDefaultMax = 16;
+
+bool use_small(const rf_ctx *c)
+{
+    if (!c->b_single || c->n > kSmallMax) return false;
+    if (c->mixed_path != 0) return c->mixed_path == 1;
+    return c->n <= kSmallDefaultMax;
+}
+
+int small_gpt(const rf_ctx *c, bool rec)
+{
+    if (rec) return 1;
+    if (c->gpt > 0) return c->gpt == 2 ? 2 : 1;
+    return c->cfg.rays_per_thread == 8 ? 2 : 1;
+}
+
+int64_t mixed_chunk_draws(const rf_ctx *c, bool rec)
+{
+    return use_small(c) ? (int64_t)kSmallThreads * small_gpt(c, rec) : (int64_t)kBatchChunkDraws;
+}
+
+// One launch of the small-scene kernel over host-planned segments (chunks of
+// kSmallThreads * gpt draws) of the scene held in the batch tables.
+rf_status run_small(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_chunks, bool rec, int32_t *d_rec,
+                    int64_t rec_base, bool zero_hits)
+{
+    c->last_launches = 0;
+    c->timed = false;
+    c->last_small = true;
+    std::fill(std::begin(c->small_work), std::end(c->small_work), 0ull);
+    if (zero_hits) RF_CUDA(c, cudaMemsetAsync(c->b_hits.p, 0, (size_t)c->b_hits_total * 8, c->stream));
+    RF_CUDA(c, cudaMemsetAsync(c->b_counters.p, 0, sizeof(BatchCounters), c->stream));
+    if (seg.empty() || total_chunks == 0) return RF_OK;
+    if (c->cfg.work_counts) {  // every ray is tested against every surface
+        int64_t rays = 0;
+        for (const Segment &sg : seg) rays += sg.ray_end - sg.ray_begin;
+        for (const rf_primitive &pr : c->prims) c->small_work[pr.type] += (unsigned long long)rays;
+    }
+    RF_CUDA(c, c->h_seg.ensure(seg.size() * sizeof(Segment)));
+    RF_CUDA(c, c->d_seg.ensure(seg.size() * sizeof(Segment)));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::memcpy(c->h_seg.p, seg.data(), seg.size() * sizeof(Segment));
+    RF_CUDA(c, cudaMemcpyAsync(c->d_seg.p, c->h_seg.p, seg.size() * sizeof(Segment), cudaMemcpyHostToDevice,
+                               c->stream));
+    TraceParams p = batch_params(c);
+    p.cmask = nullptr;
+    p.mask_off = nullptr;
+    p.n = c->b_info[0].n;
+    p.eps = c->b_info[0].eps;
+    p.seg = c->d_seg.as<Segment>();
+    p.nseg = (int32_t)seg.size();
+    p.total_chunks = total_chunks;
+    p.rec = d_rec;
+    p.rec_base = rec_base;
+    const int gpt = small_gpt(c, rec);
+    int bps = mixed_small_blocks_per_sm(gpt, rec);
+    if (bps <= 0) bps = 1;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)c->sms * bps, total_chunks));
+    RF_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    RF_CUDA(c, launch_mixed_small(p, gpt, rec, grid, c->stream));
+    RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    c->last_launches = 1;
+    c->timed = true;
+    return RF_OK;
+}
+
+// A MIXED trace of the single scene: small-scene or batched kernel.
+rf_status run_mixed(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_chunks, bool rec, int32_t *d_rec,
+                    int64_t rec_base, bool zero_hits)
+{
+    if (use_small(c)) return run_small(c, seg, total_chunks, rec, d_rec, rec_base, zero_hits);
+    c->last_small = false;
+    return run_batched(c, seg, total_chunks, rec, d_rec, rec_base, zero_hits);
 }
 
 rf_status require_scene(rf_ctx *c)
@@ -944,7 +1058,7 @@ void rf_destroy(rf_ctx *c)
     for (DevBuf *b : {&c->d_tab, &c->d_emit, &c->d_bvtab, &c->d_bvinfo, &c->d_hits, &c->d_seg,
                       &c->d_rays, &c->d_F, &c->d_rec, &c->d_err, &c->d_misc, &c->b_tab, &c->b_emit,
                       &c->b_bsph, &c->b_scenes, &c->b_hits, &c->b_rows, &c->b_counters, &c->b_patch,
-                      &c->b_chain, &c->b_plane, &c->b_cone, &c->b_maskrows, &c->b_maskoff, &c->b_mask})
+                      &c->b_chain, &c->b_plane, &c->b_cone, &c->b_maskrows, &c->b_maskoff, &c->b_mask, &c->b_frame})
         b->release();
     c->h_seg.release();
     c->h_rays.release();
@@ -1039,8 +1153,9 @@ rf_status rf_trace_async(rf_ctx *c, const int64_t *rays, int32_t use_bv)
         if (!c->b_single) return fail(c, RF_ERR_STATE, "scene not prepared for the mixed kernel");
         std::vector<Segment> seg;
         int64_t chunks = 0;
-        for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, 0, rays[e], kBatchChunkDraws, chunks);
-        if ((s = run_batched(c, seg, chunks, false, nullptr, 0, true)) != RF_OK) return s;
+        const int64_t cg = mixed_chunk_draws(c, false);
+        for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, 0, rays[e], cg, chunks);
+        if ((s = run_mixed(c, seg, chunks, false, nullptr, 0, true)) != RF_OK) return s;
         c->have_results = true;
         return RF_OK;
     }
@@ -1079,14 +1194,14 @@ rf_status rf_trace_range(rf_ctx *c, const int64_t *first_ray, const int64_t *cou
     int64_t chunks = 0;
     const bool mixed = c->cfg.precision == RF_PREC_MIXED;
     Plan pl = make_plan(c, use_bv != 0, false);
-    const int64_t chunk_gids = mixed ? kBatchChunkDraws : (int64_t)pl.lc.block * pl.lc.gpt;
+    const int64_t chunk_gids = mixed ? mixed_chunk_draws(c, false) : (int64_t)pl.lc.block * pl.lc.gpt;
     for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, first_ray[e], count[e], chunk_gids, chunks);
     if (!accumulate) c->last_rays.assign(c->n, 0);
     for (int e = 0; e < c->n; ++e) c->last_rays[e] += count[e];
     c->have_results = false;
     if (mixed) {
         if (!c->b_single) return fail(c, RF_ERR_STATE, "scene not prepared for the mixed kernel");
-        s = run_batched(c, seg, chunks, false, nullptr, 0, !accumulate);
+        s = run_mixed(c, seg, chunks, false, nullptr, 0, !accumulate);
     } else {
         s = run_trace(c, seg, chunks, pl, nullptr, 0, !accumulate);
     }
@@ -1145,6 +1260,8 @@ rf_status rf_read_results(rf_ctx *c, uint64_t *hits_out, double *F_out)
                                    sizeof c->last_work, cudaMemcpyDeviceToHost, c->stream));
     }
     RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->cfg.precision == RF_PREC_MIXED && c->last_small)
+        std::copy(std::begin(c->small_work), std::end(c->small_work), std::begin(c->last_work));
     int32_t err = 0;
     RF_CUDA(c, cudaMemcpy(&err, c->d_err.p, 4, cudaMemcpyDeviceToHost));
     if (err) return fail(c, RF_ERR_TIMEOUT, "device reported error %d", err);
@@ -1195,8 +1312,8 @@ rf_status rf_trace_rays(rf_ctx *c, int32_t emitter, int64_t first_ray, int64_t n
     if (c->cfg.precision == RF_PREC_MIXED) {
         if (use_bv) return fail(c, RF_ERR_UNSUPPORTED, "bounding-surface semantics need EXACT, FAST or FP64");
         std::vector<Segment> seg;
-        const int64_t chunks = plan_segments(seg, emitter, 0, first_ray, n_rays, kBatchChunkDraws, 0);
-        if ((s = run_batched(c, seg, chunks, true, c->d_rec.as<int32_t>(), first_ray, false)) != RF_OK) return s;
+        const int64_t chunks = plan_segments(seg, emitter, 0, first_ray, n_rays, mixed_chunk_draws(c, true), 0);
+        if ((s = run_mixed(c, seg, chunks, true, c->d_rec.as<int32_t>(), first_ray, false)) != RF_OK) return s;
     } else {
         Plan pl = make_plan(c, use_bv != 0, true);
         const int64_t chunk_gids = (int64_t)pl.lc.block * pl.lc.gpt;
@@ -1674,6 +1791,87 @@ void tune_apply(rf_ctx *c, const TuneChoice &t)
     c->stage = t.stage;
     c->order = t.order;
 }
+
+// Trial budgets of the autotuner: about 2^25 rays (the steady state of a
+// persistent wave, a few ms), spread like the last trace's budgets when there
+// was one (the workload being tuned for), else evenly.
+std::vector<int64_t> tune_budgets(const rf_ctx *c)
+{
+    const double target = (double)((int64_t)1 << 25);
+    std::vector<int64_t> rays(c->n, std::max<int64_t>(4096, ((int64_t)1 << 25) / c->n) / 4 * 4);
+    if ((int)c->last_rays.size() == c->n) {
+        double tot = 0.0;
+        for (int64_t r : c->last_rays) tot += (double)r;
+        if (tot > 0.0)
+            for (int e = 0; e < c->n; ++e) rays[e] = (int64_t)(target * (double)c->last_rays[e] / tot) / 4 * 4;
+    }
+    return rays;
+}
+
+// MIXED: a single scene of at most kSmallMax surfaces may take the small-scene
+// kernel (4 or 8 rays per thread) instead of the batched kernel; time the three
+// and keep the fastest (results are the same ray for ray: same arithmetic, and a
+// ray's result depends on the ray alone).  The choice is cached like the plain
+// kernels' (block field 1 = small-scene kernel, 2 = batched kernel).
+rf_status autotune_mixed(rf_ctx *c, const char *cache_path)
+{
+    if (!c->b_single || c->n > kSmallMax) return RF_OK;  // the batched kernel only
+    const std::string key = tune_key(c, 0);
+    TuneChoice best{};
+    bool found = false;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) { best = it->second; found = true; }
+    }
+    if (!found && cache_path && tune_lookup_file(cache_path, key, best)) {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = best;
+        found = true;
+    }
+    if (found) {
+        c->mixed_path = best.block;
+        c->gpt = best.gpt;
+        return RF_OK;
+    }
+    const std::vector<int64_t> rays = tune_budgets(c);
+    const int saved_path = c->mixed_path, saved_gpt = c->gpt;
+    double best_ms = 1e300;
+    for (int path : {2, 1})
+        for (int gpt : {1, 2}) {
+            if (path == 2 && gpt == 2) continue;
+            c->mixed_path = path;
+            c->gpt = gpt;
+            double ms_min = 1e300;
+            for (int rep = 0; rep < 3; ++rep) {
+                rf_status s = rf_trace_async(c, rays.data(), 0);
+                double ms = 0.0;
+                if (s == RF_OK) s = rf_last_trace_stats(c, &ms, nullptr);
+                if (s != RF_OK) {
+                    c->mixed_path = saved_path;
+                    c->gpt = saved_gpt;
+                    return s;
+                }
+                if (rep > 0) ms_min = std::min(ms_min, ms);  // the first run warms up
+            }
+            if (ms_min < best_ms) {
+                best_ms = ms_min;
+                best = TuneChoice{path, gpt, -1, -1, -1};
+            }
+        }
+    c->have_results = false;
+    c->mixed_path = best.block;
+    c->gpt = best.gpt;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = best;
+    }
+    if (cache_path) {
+        std::ofstream f(cache_path, std::ios::app);
+        if (f) f << key << "|" << best.block << " " << best.gpt << " -1 -1 -1\n";
+    }
+    return RF_OK;
+}
 }  // namespace
 
 rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
@@ -1682,7 +1880,10 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
     rf_status s = require_scene(c);
     if (s != RF_OK) return s;
     if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
-    if (c->cfg.precision == RF_PREC_MIXED) return RF_OK;  // one launch shape
+    if (c->cfg.precision == RF_PREC_MIXED) {
+        if (use_bv) return fail(c, RF_ERR_UNSUPPORTED, "bounding-surface semantics need EXACT, FAST or FP64");
+        return autotune_mixed(c, cache_path);
+    }
     const std::string key = tune_key(c, use_bv ? 1 : 0);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -1702,14 +1903,7 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
     // trials long enough for the steady state of a persistent wave: about 2^25
     // rays (a few ms each), spread like the last trace's budgets when there was
     // one (the workload being tuned for), else evenly
-    const double target = (double)((int64_t)1 << 25);
-    std::vector<int64_t> rays(c->n, std::max<int64_t>(4096, ((int64_t)1 << 25) / c->n) / 4 * 4);
-    if ((int)c->last_rays.size() == c->n) {
-        double tot = 0.0;
-        for (int64_t r : c->last_rays) tot += (double)r;
-        if (tot > 0.0)
-            for (int e = 0; e < c->n; ++e) rays[e] = (int64_t)(target * (double)c->last_rays[e] / tot) / 4 * 4;
-    }
+    const std::vector<int64_t> rays = tune_budgets(c);
     const bool bv = use_bv != 0;
     const bool wide = !bv && c->cfg.precision != RF_PREC_FP64;
     double best_ms = 1e300;

@@ -64,6 +64,7 @@ struct TraceParams {
     const int32_t *d_nseg;          // batched kernel: device-resident segment count (or null)
     unsigned long long *work;       // batched kernel: [0..5] ray x surface tests by type,
                                     // [6] candidate surfaces of packets, [7] packets
+    const float4 *frame;            // mixed kernels: per emitter kEmitFrameWords (planar emission frame)
     const uint32_t *cmask;          // batched kernel: cell masks of all rows that have them
     const int64_t *mask_off;        // per global row (prim_off + emitter): first mask word, -1 = none
 };
@@ -119,12 +120,23 @@ template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
 cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool count, int grid, cudaStream_t st);
 int batched_blocks_per_sm(bool rec, bool resident);
 cudaError_t launch_build_masks(const MaskInputs &in, uint32_t *out, cudaStream_t st);
+// Mixed-precision kernel for one small scene with the plain kernel's launch shape
+// (rf_kern_fast.cu): gpt Philox draws per thread, block kSmallThreads.
+constexpr int kSmallMax = 64;       // surfaces of the largest scene it takes
+constexpr int kSmallThreads = 256;
+cudaError_t launch_mixed_small(const TraceParams &p, int gpt, bool rec, int grid, cudaStream_t st);
+int mixed_small_blocks_per_sm(int gpt, bool rec);
 size_t batched_smem_bytes();
 int batched_tile();  // scenes with at most this many surfaces use the resident kernel
 constexpr int kBatchTile = 512;  // surfaces the resident kernel keeps in shared memory
 constexpr int kBatchBruteMax = 12;  // scenes up to this many surfaces are traced without culling
+constexpr int kEmitFrameWords = 5;  // float4 words of a planar emitter's frame (mixed kernels)
 constexpr int kBatchMaxSurfaces = 32767;  // nearest hits are kept as int16 in shared memory
 constexpr int kBatchChunkDraws = 8192;  // Philox draws per chunk of the batched kernel
+
+// Emission frame of an emitter for the mixed kernels (rf_capi.cu): planar
+// emitters get their origin, in-plane axes and alignment rotation in FP64.
+void emit_frame(const rf_primitive &e, float4 *out);
 
 // Host preparation of one scene for the batched kernel (rf_capi.cu); eps_out
 // receives the scene's self-hit threshold for the configured eps.

@@ -3,6 +3,7 @@
 // default contraction of products and sums into FMA.
 #include "rf_trace_kernels.cuh"
 #include "rf_batched.cuh"
+#include "rf_mixed_small.cuh"
 
 namespace rf {
 template cudaError_t launch_trace<MFast>(const LaunchCfg &, const TraceParams &, cudaStream_t);
@@ -57,5 +58,33 @@ cudaError_t launch_build_masks(const MaskInputs &in, uint32_t *out, cudaStream_t
 }
 
 int batched_tile() { return kBatchTile; }
+
+template <int GPT, bool REC>
+static cudaError_t launch_s(const TraceParams &p, int grid, cudaStream_t st)
+{
+    mixed_small_kernel<GPT, REC><<<grid, kSmallThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_small(const TraceParams &p, int gpt, bool rec, int grid, cudaStream_t st)
+{
+    if (p.n <= 0 || p.n > kSmallMax) return cudaErrorInvalidValue;
+    if (rec) return launch_s<1, true>(p, grid, st);
+    return gpt == 2 ? launch_s<2, false>(p, grid, st) : launch_s<1, false>(p, grid, st);
+}
+
+template <int GPT, bool REC>
+static int occ_s()
+{
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mixed_small_kernel<GPT, REC>, kSmallThreads, 0);
+    return nb;
+}
+
+int mixed_small_blocks_per_sm(int gpt, bool rec)
+{
+    if (rec) return occ_s<1, true>();
+    return gpt == 2 ? occ_s<2, false>() : occ_s<1, false>();
+}
 
 }  // namespace rf

@@ -36,9 +36,11 @@ constexpr size_t kOffSeg = 512;                                      // kMaxPrim
 constexpr size_t kOffTab = kOffSeg + sizeof(Segment) * kMaxPrims;    // hit records
 constexpr size_t kOffEmit = kOffTab + sizeof(HitRec) * kMaxPrims;    // emitter records
 constexpr size_t kOffSph = kOffEmit + sizeof(rf_primitive) * kMaxPrims;  // bounding spheres
-constexpr size_t kScratchUsed = kOffSph + sizeof(float4) * kMaxPrims;
+constexpr size_t kOffFrame = kOffSph + sizeof(float4) * kMaxPrims;      // planar emission frames
+constexpr size_t kScratchUsed = kOffFrame + sizeof(float4) * kEmitFrameWords * kMaxPrims;
 static_assert(kScratchUsed <= RF_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the stated size");
-static_assert(kOffTab % 16 == 0 && kOffEmit % 16 == 0 && kOffSph % 16 == 0, "16-byte alignment");
+static_assert(kOffTab % 16 == 0 && kOffEmit % 16 == 0 && kOffSph % 16 == 0 && kOffFrame % 16 == 0,
+              "16-byte alignment");
 
 struct Counters {
     unsigned long long queue;
@@ -59,6 +61,7 @@ unsigned char *g_dev[kMaxDevices] = {};
 rf_primitive h_emit[kMaxPrims];
 HitRec h_tab[kMaxPrims];
 float4 h_sph[kMaxPrims];
+float4 h_frame[kMaxPrims * kEmitFrameWords];
 Segment h_seg[kMaxPrims];
 
 bool finite12(const float *v)
@@ -101,6 +104,7 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
 
     float seps = eps;  // eps < 0: relative to the scene's size, like rf_trace
     prepare_mixed_tables(prims, n, eps, h_emit, h_tab, h_sph, &seps);
+    for (int i = 0; i < n; ++i) emit_frame(h_emit[i], h_frame + (size_t)i * kEmitFrameWords);
     int nseg = 0;
     int64_t chunks = 0;
     for (int e = 0; e < n; ++e) {
@@ -132,6 +136,8 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(base + kOffEmit, h_emit, sizeof(rf_primitive) * n, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + kOffSph, h_sph, sizeof(float4) * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + kOffFrame, h_frame, sizeof(float4) * kEmitFrameWords * n, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return RF_ERR_CUDA;
     if (chunks == 0) return RF_OK;
 
@@ -140,6 +146,7 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     p.tab = reinterpret_cast<const HitRec *>(base + kOffTab);
     p.emit = reinterpret_cast<const rf_primitive *>(base + kOffEmit);
     p.bsph = reinterpret_cast<const float4 *>(base + kOffSph);
+    p.frame = reinterpret_cast<const float4 *>(base + kOffFrame);
     p.scenes = reinterpret_cast<const SceneInfo *>(base + kOffScene);
     p.seg = reinterpret_cast<const Segment *>(base + kOffSeg);
     p.hits = reinterpret_cast<unsigned long long *>(hits_dev);

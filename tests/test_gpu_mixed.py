@@ -306,3 +306,35 @@ def test_mixed_results_independent_of_scheduling(built_lib, name):
                 assert int(w.sum()) == 0
     for h in runs[1:]:
         assert np.array_equal(h, runs[0])
+
+
+@pytest.mark.parametrize("name", ["gen_enclosure3", "input-C47", "input-C122", "gen_precision_stress"])
+def test_small_scene_kernel_equals_batched(built_lib, name):
+    """Single scenes of at most 16 surfaces take the small-scene kernel (the plain
+    kernel's launch shape); the same scene as a one-scene batch takes the batched
+    kernel.  Same emission, tests and per-ray resolution: identical tallies, with
+    4 and 8 rays per thread."""
+    sc = golden_scene(name)
+    assert sc.n <= 16
+    rng = np.random.default_rng(9)
+    rays = (rng.integers(1, 300000, sc.n) * 4 + rng.integers(0, 4, sc.n)).astype(np.int64)
+    with Tracer(precision=PREC_MIXED) as t:
+        hb, _ = t.trace_batch([sc], [rays])
+    for rpt in (4, 8):
+        with _tracer(sc, precision=PREC_MIXED, rays_per_thread=rpt, work_counts=True) as t:
+            hs, _ = t.trace(rays)
+            w = t.work_counts()
+        assert np.array_equal(hs, hb[0]), (name, rpt)
+        assert int(w[:6].sum()) == int(rays.sum()) * sc.n  # every ray against every surface
+
+
+def test_mixed_autotune_keeps_results(built_lib):
+    """rf_autotune times the small-scene and the batched kernel for a small scene
+    and keeps the faster; tallies are the same either way."""
+    sc = golden_scene("gen_enclosure3")
+    rays = np.full(sc.n, 400_004, np.int64)
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        h0, _ = t.trace(rays)
+        t.autotune()
+        h1, _ = t.trace(rays)
+    assert np.array_equal(h0, h1)
