@@ -74,6 +74,8 @@ struct BatchSmem {
     int hist[kBatchHist];
     rf_primitive emit;
     float4 frame[kFrameWords];
+    HitRec bvtab[kBatchMaxBV];          // bounding surfaces (runBVGPU semantics)
+    int4 bvinfo[kBatchMaxBV];           // (settings, first child, end of children, 0)
     int64_t chunk;
     int next_packet;
     int n_valid;
@@ -397,13 +399,13 @@ __device__ __forceinline__ bool own_gate(const uint32_t *mcell, int j, const Ray
 // Full nearest-hit search for one ray over the surfaces its gate admits, with
 // FP64 for every ill-conditioned quadric (cold path: the ray deferred more than
 // one test, and a lane keeps only one).
-__device__ __noinline__ int retrace_f64(int n, bool resident, const HitRec *stab, const HitRec *gtab,
+__device__ __noinline__ int retrace_f64(int lo, int hi, bool resident, const HitRec *stab, const HitRec *gtab,
                                         const float4 *sbs, const float4 *gbs, const uint32_t *mcell,
                                         const Ray<float> &ray, float idd, float eps, bool sc, int skip)
 {
     float tb = MFast::inf();
     int bi = -1;
-    for (int j = 0; j < n; ++j) {
+    for (int j = lo; j < hi; ++j) {
         if (j == skip || !own_gate(mcell, j, ray, idd, resident ? sbs[j] : __ldg(gbs + j))) continue;
         const HitRec h = resident ? stab[j] : load_rec(gtab, j);
         bool defer = false;
@@ -414,14 +416,15 @@ __device__ __noinline__ int retrace_f64(int n, bool resident, const HitRec *stab
     return bi;
 }
 
-// Nearest hit of a ray tested against all n surfaces: bi / tb from the index-order
+// Nearest hit of a ray tested against all surfaces [lo, hi): bi / tb from the index-order
 // loop, dj the deferred test (-1 none, j the only one, -2 several).  One deferral
 // is re-evaluated in FP64 (lower index wins a tie: it ran out of order); several
 // re-trace the ray with FP64 for each.  Shared by the small-scene paths of the
 // batched kernel and of mixed_small_kernel, so both give the same result.
-__device__ __forceinline__ int resolve_brute(int bi, float tb, int dj, int n, bool resident, const HitRec *stab,
-                                             const HitRec *gtab, const float4 *sbs, const float4 *gbs,
-                                             const Ray<float> &ray, float eps, bool sc, int skip, int &nref)
+__device__ __forceinline__ int resolve_brute(int bi, float tb, int dj, int lo, int hi, bool resident,
+                                             const HitRec *stab, const HitRec *gtab, const float4 *sbs,
+                                             const float4 *gbs, const Ray<float> &ray, float eps, bool sc, int skip,
+                                             int &nref)
 {
     if (dj >= 0) {
         const HitRec hq = resident ? stab[dj] : load_rec(gtab, dj);
@@ -429,18 +432,56 @@ __device__ __forceinline__ int resolve_brute(int bi, float tb, int dj, int n, bo
         if (t < tb || (t == tb && bi >= 0 && dj < bi)) bi = dj;
         ++nref;
     } else if (dj == -2) {
-        bi = retrace_f64(n, resident, stab, gtab, sbs, gbs, nullptr, ray,
+        bi = retrace_f64(lo, hi, resident, stab, gtab, sbs, gbs, nullptr, ray,
                          MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz), eps, sc, skip);
         nref += 2;
     }
     return bi;
 }
 
+// The bounding-surface walk of runBVGPU (RayFactorGPU.cl:580-619) for one ray:
+// surfaces w = 0..nbv-1 in order, each tested in mixed precision (FP64 when
+// ill-conditioned); find(lo, hi) is the ray's nearest hit among the children
+// [lo, hi) (findObject, :445-472).  It is called for every w, in every lane,
+// before the lane's own decision, so kernels whose find() is warp-wide stay in
+// step.  stale: RF_COMPAT_BV_STALE, where a plain bounding surface that becomes
+// the nearest keeps the child found under an earlier one (:596-619).
+template <class Find>
+__device__ __forceinline__ int bv_select(const HitRec *bvtab, const int4 *bvinfo, int nbv, const Ray<float> &ray,
+                                         float eps, bool sc, bool stale, Find find)
+{
+    float tbest = MFast::inf();
+    int bvi = -1, obj = -1, nb = -1;  // nb: children's nearest hit of the current winner bvi
+    for (int w = 0; w < nbv; ++w) {
+        const HitRec hb = bvtab[w];
+        bool defer = false;
+        float t = hit_mixed(__float_as_int(hb.aux.x), hb, ray, eps, sc, defer);
+        if (defer) t = hit_f64(hb, ray, eps, sc);
+        const int4 info = bvinfo[w];
+        const int nw = find(info.y, info.z);
+        if (t < tbest) {
+            if (info.x == 1) {  // test the children at once; the surface counts only if one is hit
+                obj = nw;
+                if (nw != -1) { tbest = t; bvi = w; nb = nw; }
+            } else {
+                tbest = t;
+                bvi = w;
+                nb = nw;
+                if (!stale) obj = -1;
+            }
+        }
+    }
+    if (bvi != -1 && obj == -1) obj = nb;  // the winner's children
+    return obj;
+}
+
 // RESIDENT: every scene of the launch fits the shared-memory tables
 // (n <= kBatchTile); otherwise surfaces are read through L1.  COUNT: also count
 // the tests by surface type, the candidates and the packets (p.work); the
-// counters cost a few per cent, so timed runs leave them out.
-template <bool REC, bool RESIDENT, bool COUNT>
+// counters cost a few per cent, so timed runs leave them out.  BV: one resident
+// scene with bounding surfaces (p.bvtab, p.bvinfo, p.nbv <= kBatchMaxBV) traced
+// with runBVGPU's semantics (bv_select).
+template <bool REC, bool RESIDENT, bool COUNT, bool BV>
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TraceParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -517,6 +558,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     for (int i = tid; i < 4 * si.n; i += blockDim.x) dst[i] = __ldg(src + i);
                     for (int i = tid; i < si.n; i += blockDim.x) S.bs[i] = __ldg(p.bsph + si.prim_off + i);
                 }
+                if (BV) {
+                    for (int i = tid; i < 4 * p.nbv; i += blockDim.x)
+                        reinterpret_cast<float4 *>(S.bvtab)[i] = __ldg(reinterpret_cast<const float4 *>(p.bvtab) + i);
+                    for (int i = tid; i < p.nbv; i += blockDim.x) S.bvinfo[i] = __ldg(p.bvinfo + i);
+                }
                 cur_scene = sg.scene;
             }
             if (tid < (int)(sizeof(rf_primitive) / 4))
@@ -537,10 +583,10 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
         const uint32_t sid = (p.compat & RF_COMPAT_STREAMS) ? 0u : (p.scene_id + (uint32_t)sg.scene);
         const HitRec *gtab = p.tab + si.prim_off;
         unsigned long long *grow = p.hits + si.hits_off + (int64_t)cur_emitter * si.n;
-        const int skip = self_skip(S.emit, cur_emitter);  // block-uniform
 
         if (si.n <= kBruteMax) {  // block-uniform: too few surfaces for culling to pay
             // every thread traces its own rays against all surfaces in index order
+            const int skip = self_skip(S.emit, cur_emitter);  // block-uniform
             uint32_t nv_warp = 0;
 #pragma unroll 1
             for (int g = 0; g < kBatchDraws; ++g) {
@@ -554,7 +600,27 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     const int64_t rid = gid * 4 + v;
                     const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
                     int bi = -1;
-                    if (valid) {
+                    if (valid && BV) {
+                        float r[4];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
+                        const Ray<float> ray = emit_mixed(S.emit, S.frame, r);
+                        auto find = [&](int lo, int hi) {  // every child of [lo, hi), index order
+                            float tr = MFast::inf();
+                            int br = -1, dr = -1;
+                            for (int j = lo; j < hi; ++j) {
+                                if (j == skip) continue;
+                                const HitRec h = S.tab[j];
+                                bool defer = false;
+                                const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
+                                if (t < tr) { tr = t; br = j; }
+                                dr = defer ? (dr == -1 ? j : -2) : dr;
+                            }
+                            return resolve_brute(br, tr, dr, lo, hi, true, S.tab, gtab, S.bs, p.bsph + si.prim_off, ray,
+                                                 eps, sc, skip, nref);
+                        };
+                        bi = bv_select(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0, find);
+                    } else if (valid) {
                         float r[4];
 #pragma unroll
                         for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
@@ -570,7 +636,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             if (t < tb) { tb = t; bi = j; }
                             dj = defer ? (dj == -1 ? j : -2) : dj;
                         }
-                        bi = resolve_brute(bi, tb, dj, si.n, RESIDENT, S.tab, gtab, S.bs, p.bsph + si.prim_off,
+                        bi = resolve_brute(bi, tb, dj, 0, si.n, RESIDENT, S.tab, gtab, S.bs, p.bsph + si.prim_off,
                                            ray, eps, sc, skip, nref);
                     }
                     // all 32 lanes reach the warp-wide calls below
@@ -705,83 +771,142 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 const Ray<float> ray = emit_mixed(S.emit, S.frame, r);
                 const float idd = MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
                 const uint32_t *mcell = mrow ? mrow + (int64_t)ray_key(ray, r) * nwords_all : nullptr;
-                float tb = MFast::inf();
-                int dj = -1, ndef = 0;  // deferred FP64 tests of this lane: the last one, and how many
-                if (COUNT && lane == 0) S.wcount[warp][7] += 1;
-                // surfaces in blocks of 1024 (one block when the scene has masks)
-#pragma unroll 1
-                for (int j0 = 0; j0 < si.n; j0 += 1024) {
-                    const int nwords = min(32, (si.n - j0 + 31) >> 5);
-                    unsigned cmask = 0u;  // without masks: lane w holds candidate word w
-                    if (!mcell) {  // block-uniform
+                if constexpr (BV) {
+                    // runBVGPU: the nearest child in each bounding surface's range with the
+                    // packet's culled candidate loop restricted to the range, then the walk
+                    const int skip = self_skip(S.emit, cur_emitter);
+                    unsigned cmask = 0u;  // without masks: lane w holds candidate word w (n <= kBatchTile)
+                    if (!mcell) {
                         const Packet pk = packet_bounds(ray, idd);
 #pragma unroll 1
-                        for (int w = 0; w < nwords; ++w) {
-                            const int js = j0 + (w << 5) + lane;
-                            bool cand = false;
-                            if (js < si.n) cand = packet_may_hit(pk, resident ? S.bs[js] : __ldg(gbs + js));
+                        for (int w = 0; w < nwords_all; ++w) {
+                            const int js = (w << 5) + lane;
+                            const bool cand = js < si.n && packet_may_hit(pk, S.bs[js]);
                             const unsigned cm = __ballot_sync(0xffffffffu, cand);
                             if (lane == w) cmask = cm;
                         }
                     }
+                    auto find = [&](int lo, int hi) {  // warp-wide: every lane, same lo and hi
+                        float tr = MFast::inf();
+                        int br = -1, dr = -1, nd = 0;
 #pragma unroll 1
-                    for (int w = 0; w < nwords; ++w) {
-                        const int jw = j0 + (w << 5);
-                        const unsigned cm0 = mcell ? __reduce_or_sync(0xffffffffu, __ldg(mcell + (jw >> 5)))
-                                                   : __shfl_sync(0xffffffffu, cmask, w);  // block-uniform choice
-                        unsigned cm = cm0 & ~((skip >= jw && skip < jw + 32) ? (1u << (skip - jw)) : 0u);
-                        if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
-                        // two candidates per pass: their sphere checks are independent
-                        // chains (latency hidden); tests still run in index order
-                        while (cm) {  // cm is the same in every lane
-                            const int ba_ = __ffs(cm) - 1;
-                            cm &= cm - 1;
-                            const int bb_ = cm ? __ffs(cm) - 1 : -1;
-                            cm &= cm - 1;  // 0 stays 0
-                            const int ja = jw + ba_, jb = jw + (bb_ >= 0 ? bb_ : ba_);
-                            const float4 sa = resident ? S.bs[ja] : __ldg(gbs + ja);
-                            const float4 sb = resident ? S.bs[jb] : __ldg(gbs + jb);
-                            const bool ma = ray_may_hit(ray, idd, sa);
-                            const bool mb = bb_ >= 0 && ray_may_hit(ray, idd, sb);
-                            const unsigned va = __ballot_sync(0xffffffffu, ma);
-                            const unsigned vb = __ballot_sync(0xffffffffu, mb);
-#pragma unroll
-                            for (int q = 0; q < 2; ++q) {
-                                if (!(q ? vb : va)) continue;  // warp-uniform
-                                const int j = q ? jb : ja;
-                                const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
-                                const int type = __float_as_int(h.aux.x);
-                                if (COUNT) tcount += lane == type ? nvalid : 0;
+                        for (int w = lo >> 5; lo < hi && w <= (hi - 1) >> 5; ++w) {
+                            const int jw = w << 5;
+                            unsigned cm = mcell ? __reduce_or_sync(0xffffffffu, __ldg(mcell + w))
+                                                : __shfl_sync(0xffffffffu, cmask, w);
+                            if (lo > jw) cm &= ~0u << (lo - jw);
+                            if (hi < jw + 32) cm &= (1u << (hi - jw)) - 1u;
+                            if (skip >= jw && skip < jw + 32) cm &= ~(1u << (skip - jw));
+                            while (cm) {
+                                const int j = jw + __ffs(cm) - 1;
+                                cm &= cm - 1;
+                                if (!__any_sync(0xffffffffu, ray_may_hit(ray, idd, S.bs[j]))) continue;
+                                const HitRec h = S.tab[j];
                                 bool defer = false;
-                                const float t = hit_mixed(type, h, ray, eps, sc, defer);
-                                if (t < tb) { tb = t; bi = j; }
-                                ndef += defer;  // predicated, no branch
-                                dj = defer ? j : dj;
+                                const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
+                                if (t < tr) { tr = t; br = j; }
+                                nd += defer;
+                                dr = defer ? j : dr;
+                            }
+                        }
+                        // as below: nearest among the children the lane's own gate admits
+                        bool again = valid && nd > 1;
+                        if (valid && nd == 1) {
+                            const float t = hit_f64(S.tab[dr], ray, eps, sc);
+                            if (t < tr || (t == tr && br >= 0 && dr < br)) { tr = t; br = dr; }
+                            ++nref;
+                            again = !own_gate(mcell, dr, ray, idd, S.bs[dr]);
+                        }
+                        if (valid && !again && br >= 0) again = !own_gate(mcell, br, ray, idd, S.bs[br]);
+                        if (again) {
+                            br = retrace_f64(lo, hi, true, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc, skip);
+                            nref += 2;
+                        }
+                        return br;
+                    };
+                    bi = bv_select(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0, find);
+                } else {
+                    float tb = MFast::inf();
+                    int dj = -1, ndef = 0;  // deferred FP64 tests of this lane: the last one, and how many
+                    if (COUNT && lane == 0) S.wcount[warp][7] += 1;
+                    // surfaces in blocks of 1024 (one block when the scene has masks)
+#pragma unroll 1
+                    for (int j0 = 0; j0 < si.n; j0 += 1024) {
+                        const int nwords = min(32, (si.n - j0 + 31) >> 5);
+                        unsigned cmask = 0u;  // without masks: lane w holds candidate word w
+                        if (!mcell) {  // block-uniform
+                            const Packet pk = packet_bounds(ray, idd);
+                            const int self = self_skip(S.emit, cur_emitter);  // (masks leave it out already)
+#pragma unroll 1
+                            for (int w = 0; w < nwords; ++w) {
+                                const int js = j0 + (w << 5) + lane;
+                                bool cand = false;
+                                if (js < si.n && js != self)
+                                    cand = packet_may_hit(pk, resident ? S.bs[js] : __ldg(gbs + js));
+                                const unsigned cm = __ballot_sync(0xffffffffu, cand);
+                                if (lane == w) cmask = cm;
+                            }
+                        }
+#pragma unroll 1
+                        for (int w = 0; w < nwords; ++w) {
+                            const int jw = j0 + (w << 5);
+                            const unsigned cm0 = mcell ? __reduce_or_sync(0xffffffffu, __ldg(mcell + (jw >> 5)))
+                                                       : __shfl_sync(0xffffffffu, cmask, w);  // block-uniform choice
+                            unsigned cm = cm0;
+                            if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
+                            // two candidates per pass: their sphere checks are independent
+                            // chains (latency hidden); tests still run in index order
+                            while (cm) {  // cm is the same in every lane
+                                const int ba_ = __ffs(cm) - 1;
+                                cm &= cm - 1;
+                                const int bb_ = cm ? __ffs(cm) - 1 : -1;
+                                cm &= cm - 1;  // 0 stays 0
+                                const int ja = jw + ba_, jb = jw + (bb_ >= 0 ? bb_ : ba_);
+                                const float4 sa = resident ? S.bs[ja] : __ldg(gbs + ja);
+                                const float4 sb = resident ? S.bs[jb] : __ldg(gbs + jb);
+                                const bool ma = ray_may_hit(ray, idd, sa);
+                                const bool mb = bb_ >= 0 && ray_may_hit(ray, idd, sb);
+                                const unsigned va = __ballot_sync(0xffffffffu, ma);
+                                const unsigned vb = __ballot_sync(0xffffffffu, mb);
+#pragma unroll
+                                for (int q = 0; q < 2; ++q) {
+                                    if (!(q ? vb : va)) continue;  // warp-uniform
+                                    const int j = q ? jb : ja;
+                                    const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
+                                    const int type = __float_as_int(h.aux.x);
+                                    if (COUNT) tcount += lane == type ? nvalid : 0;
+                                    bool defer = false;
+                                    const float t = hit_mixed(type, h, ray, eps, sc, defer);
+                                    if (t < tb) { tb = t; bi = j; }
+                                    ndef += defer;  // predicated, no branch
+                                    dj = defer ? j : dj;
+                                }
                             }
                         }
                     }
-                }
-                // The lane's result must be its nearest hit among the surfaces its own
-                // gate admits (the set its cell mask and sphere check select), which
-                // depends on the ray alone.  The loop above took the nearest over the
-                // packet's tested surfaces, a superset; when the winner passes the
-                // lane's gate it is also the nearest of the gated set (same index-order
-                // ties), otherwise -- or when the lane deferred more than one test --
-                // the lane re-traces over its gated set (cold).  A single deferred test
-                // is re-evaluated in FP64 (lower index wins a tie: it ran out of order).
-                bool retrace = valid && ndef > 1;
-                if (valid && ndef == 1) {
-                    const HitRec hq = RESIDENT ? S.tab[dj] : load_rec(gtab, dj);
-                    const float t = hit_f64(hq, ray, eps, sc);
-                    if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
-                    ++nref;
-                    retrace = !own_gate(mcell, dj, ray, idd, resident ? S.bs[dj] : __ldg(gbs + dj));
-                }
-                if (valid && !retrace && bi >= 0)
-                    retrace = !own_gate(mcell, bi, ray, idd, resident ? S.bs[bi] : __ldg(gbs + bi));
-                if (retrace) {
-                    bi = retrace_f64(si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc, skip);
-                    nref += 2;
+                    // The lane's result must be its nearest hit among the surfaces its own
+                    // gate admits (the set its cell mask and sphere check select), which
+                    // depends on the ray alone.  The loop above took the nearest over the
+                    // packet's tested surfaces, a superset; when the winner passes the
+                    // lane's gate it is also the nearest of the gated set (same index-order
+                    // ties), otherwise -- or when the lane deferred more than one test --
+                    // the lane re-traces over its gated set (cold).  A single deferred test
+                    // is re-evaluated in FP64 (lower index wins a tie: it ran out of order).
+                    bool retrace = valid && ndef > 1;
+                    if (valid && ndef == 1) {
+                        const HitRec hq = RESIDENT ? S.tab[dj] : load_rec(gtab, dj);
+                        const float t = hit_f64(hq, ray, eps, sc);
+                        if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
+                        ++nref;
+                        retrace = !own_gate(mcell, dj, ray, idd, resident ? S.bs[dj] : __ldg(gbs + dj));
+                    }
+                    if (valid && !retrace && bi >= 0)
+                        retrace = !own_gate(mcell, bi, ray, idd, resident ? S.bs[bi] : __ldg(gbs + bi));
+                    if (retrace) {
+                        bi = retrace_f64(0, si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc,
+                                         self_skip(S.emit, cur_emitter));
+                        nref += 2;
+                    }
                 }
                 if (REC && valid) p.rec[gid0 * 4 + l - p.rec_base] = bi;
             }
@@ -866,7 +991,9 @@ __global__ void __launch_bounds__(256) build_masks_kernel(MaskInputs in, uint32_
             if (sph.w < 0.0f) break;
             ok = cell_reaches(ball, ac, sin_t, sph);
         }
-        if (ok && plane_separates(ball, ac, sin_t, in.plane[gj])) ok = false;
+        const float4 pl = in.plane[gj];
+        if (ok && plane_separates(ball, ac, sin_t, pl)) ok = false;
+        if (j == row.emitter && pl.w == pl.w) ok = false;  // a planar emitter cannot hit itself (self_skip)
         bits |= (ok ? 1u : 0u) << b;
     }
     out[t] = bits;

@@ -119,6 +119,7 @@ struct rf_ctx {
     DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters;
     // cell masks of the batched kernel and their inputs (built at upload)
     DevBuf b_patch, b_chain, b_plane, b_cone, b_maskrows, b_maskoff, b_mask, b_frame;
+    DevBuf b_bvtab, b_bvinfo;  // the single scene's bounding surfaces, re-centred like its surfaces
     bool b_masks = false;
     double b_mask_ms = 0.0;     // device time of the last mask build
     std::vector<SceneInfo> b_info;
@@ -858,7 +859,7 @@ int batched_grid(rf_ctx *c, bool rec)
 
 // One persistent launch over host-planned segments.
 rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_chunks, bool rec,
-                      int32_t *d_rec, int64_t rec_base, bool zero_hits)
+                      int32_t *d_rec, int64_t rec_base, bool zero_hits, bool bv = false)
 {
     c->last_small = false;
     c->last_launches = 0;
@@ -880,7 +881,14 @@ rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_
     p.rec_base = rec_base;
     const int grid = (int)std::min<int64_t>(batched_grid(c, rec), total_chunks);
     RF_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    RF_CUDA(c, launch_batched(p, rec, batch_resident(c), c->cfg.work_counts != 0, grid, c->stream));
+    if (bv) {
+        p.bvtab = c->b_bvtab.as<HitRec>();
+        p.bvinfo = c->b_bvinfo.as<int4>();
+        p.nbv = c->nbv;
+        RF_CUDA(c, launch_batched_bv(p, rec, grid, c->stream));
+    } else {
+        RF_CUDA(c, launch_batched(p, rec, batch_resident(c), c->cfg.work_counts != 0, grid, c->stream));
+    }
     RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     c->last_launches = 1;
     c->timed = true;
@@ -905,9 +913,9 @@ int small_gpt(const rf_ctx *c, bool rec)
     return c->cfg.rays_per_thread == 8 ? 2 : 1;
 }
 
-int64_t mixed_chunk_draws(const rf_ctx *c, bool rec)
+int64_t mixed_chunk_draws(const rf_ctx *c, bool rec, bool bv)
 {
-    return use_small(c) ? (int64_t)kSmallThreads * small_gpt(c, rec) : (int64_t)kBatchChunkDraws;
+    return !bv && use_small(c) ? (int64_t)kSmallThreads * small_gpt(c, rec) : (int64_t)kBatchChunkDraws;
 }
 
 // One launch of the small-scene kernel over host-planned segments (chunks of
@@ -955,13 +963,26 @@ rf_status run_small(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_ch
     return RF_OK;
 }
 
-// A MIXED trace of the single scene: small-scene or batched kernel.
+// A MIXED trace of the single scene: small-scene or batched kernel; with its
+// bounding surfaces (runBVGPU semantics), the batched kernel's BV variant.
 rf_status run_mixed(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_chunks, bool rec, int32_t *d_rec,
-                    int64_t rec_base, bool zero_hits)
+                    int64_t rec_base, bool zero_hits, bool bv)
 {
+    if (bv) return run_batched(c, seg, total_chunks, rec, d_rec, rec_base, zero_hits, true);
     if (use_small(c)) return run_small(c, seg, total_chunks, rec, d_rec, rec_base, zero_hits);
-    c->last_small = false;
     return run_batched(c, seg, total_chunks, rec, d_rec, rec_base, zero_hits);
+}
+
+// Can the mixed kernel trace this scene with its bounding surfaces?
+rf_status check_mixed_bv(rf_ctx *c)
+{
+    if (c->nbv > kBatchMaxBV)
+        return fail(c, RF_ERR_UNSUPPORTED, "the mixed-precision kernel takes at most %d bounding surfaces (scene: %d)",
+                    kBatchMaxBV, c->nbv);
+    if (c->n > batched_tile())
+        return fail(c, RF_ERR_UNSUPPORTED, "bounding surfaces with the mixed-precision kernel: at most %d surfaces",
+                    batched_tile());
+    return RF_OK;
 }
 
 rf_status require_scene(rf_ctx *c)
@@ -1058,7 +1079,8 @@ void rf_destroy(rf_ctx *c)
     for (DevBuf *b : {&c->d_tab, &c->d_emit, &c->d_bvtab, &c->d_bvinfo, &c->d_hits, &c->d_seg,
                       &c->d_rays, &c->d_F, &c->d_rec, &c->d_err, &c->d_misc, &c->b_tab, &c->b_emit,
                       &c->b_bsph, &c->b_scenes, &c->b_hits, &c->b_rows, &c->b_counters, &c->b_patch,
-                      &c->b_chain, &c->b_plane, &c->b_cone, &c->b_maskrows, &c->b_maskoff, &c->b_mask, &c->b_frame})
+                      &c->b_chain, &c->b_plane, &c->b_cone, &c->b_maskrows, &c->b_maskoff, &c->b_mask, &c->b_frame, &c->b_bvtab,
+                      &c->b_bvinfo})
         b->release();
     c->h_seg.release();
     c->h_rays.release();
@@ -1132,6 +1154,28 @@ rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf
         rf_scene_desc d{prims, n, 0, nullptr};
         if ((st = upload_batch(c, &d, 1, false)) != RF_OK) return st;
         c->b_single = true;
+        if (nbv > 0) {  // bounding surfaces in the surfaces' re-centred frame (prepare_mixed's anchor)
+            double a[3] = {0, 0, 0};
+            for (int i = 0; i < n; ++i)
+                for (int k = 0; k < 3; ++k) a[k] += prims[i].m[4 * k + 3];
+            for (int k = 0; k < 3; ++k) a[k] /= n;
+            std::vector<HitRec> rb(nbv);
+            for (int b = 0; b < nbv; ++b) {
+                float im[12];
+                std::memcpy(im, bvs[b].invm, sizeof im);
+                for (int k = 0; k < 3; ++k) {
+                    const float *r = bvs[b].invm + 4 * k;
+                    im[4 * k + 3] = (float)((double)r[3] + (double)r[0] * a[0] + (double)r[1] * a[1] + (double)r[2] * a[2]);
+                }
+                rb[b] = make_hitrec(im, bvs[b].type, bvs[b].util1, bvs[b].util2);
+            }
+            RF_CUDA(c, c->b_bvtab.ensure(sizeof(HitRec) * nbv));
+            RF_CUDA(c, c->b_bvinfo.ensure(sizeof(int4) * nbv));
+            RF_CUDA(c, cudaMemcpyAsync(c->b_bvtab.p, rb.data(), sizeof(HitRec) * nbv, cudaMemcpyHostToDevice, c->stream));
+            RF_CUDA(c, cudaMemcpyAsync(c->b_bvinfo.p, bvinfo.data(), sizeof(int4) * nbv, cudaMemcpyHostToDevice,
+                                       c->stream));
+            RF_CUDA(c, cudaStreamSynchronize(c->stream));
+        }
     }
     return RF_OK;
 }
@@ -1148,14 +1192,13 @@ rf_status rf_trace_async(rf_ctx *c, const int64_t *rays, int32_t use_bv)
     c->last_rays.assign(rays, rays + c->n);
     c->have_results = false;
     if (c->cfg.precision == RF_PREC_MIXED) {
-        if (use_bv) return fail(c, RF_ERR_UNSUPPORTED, "the mixed-precision kernel culls by bounding spheres; "
-                                                    "bounding-surface semantics need EXACT, FAST or FP64");
+        if (use_bv && (s = check_mixed_bv(c)) != RF_OK) return s;
         if (!c->b_single) return fail(c, RF_ERR_STATE, "scene not prepared for the mixed kernel");
         std::vector<Segment> seg;
         int64_t chunks = 0;
-        const int64_t cg = mixed_chunk_draws(c, false);
+        const int64_t cg = mixed_chunk_draws(c, false, use_bv != 0);
         for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, 0, rays[e], cg, chunks);
-        if ((s = run_mixed(c, seg, chunks, false, nullptr, 0, true)) != RF_OK) return s;
+        if ((s = run_mixed(c, seg, chunks, false, nullptr, 0, true, use_bv != 0)) != RF_OK) return s;
         c->have_results = true;
         return RF_OK;
     }
@@ -1177,8 +1220,7 @@ rf_status rf_trace_range(rf_ctx *c, const int64_t *first_ray, const int64_t *cou
     if (s != RF_OK) return s;
     if (!first_ray || !count) return fail(c, RF_ERR_INVALID_ARG, "first_ray / count is NULL");
     if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
-    if (use_bv && c->cfg.precision == RF_PREC_MIXED)
-        return fail(c, RF_ERR_UNSUPPORTED, "bounding-surface semantics need EXACT, FAST or FP64");
+    if (use_bv && c->cfg.precision == RF_PREC_MIXED && (s = check_mixed_bv(c)) != RF_OK) return s;
     if (accumulate && (int)c->last_rays.size() != c->n)
         return fail(c, RF_ERR_STATE, "nothing to accumulate into: trace or rf_set_tallies first");
     std::vector<int64_t> ends(c->n);
@@ -1194,14 +1236,14 @@ rf_status rf_trace_range(rf_ctx *c, const int64_t *first_ray, const int64_t *cou
     int64_t chunks = 0;
     const bool mixed = c->cfg.precision == RF_PREC_MIXED;
     Plan pl = make_plan(c, use_bv != 0, false);
-    const int64_t chunk_gids = mixed ? mixed_chunk_draws(c, false) : (int64_t)pl.lc.block * pl.lc.gpt;
+    const int64_t chunk_gids = mixed ? mixed_chunk_draws(c, false, use_bv != 0) : (int64_t)pl.lc.block * pl.lc.gpt;
     for (int e = 0; e < c->n; ++e) chunks = plan_segments(seg, e, 0, first_ray[e], count[e], chunk_gids, chunks);
     if (!accumulate) c->last_rays.assign(c->n, 0);
     for (int e = 0; e < c->n; ++e) c->last_rays[e] += count[e];
     c->have_results = false;
     if (mixed) {
         if (!c->b_single) return fail(c, RF_ERR_STATE, "scene not prepared for the mixed kernel");
-        s = run_mixed(c, seg, chunks, false, nullptr, 0, !accumulate);
+        s = run_mixed(c, seg, chunks, false, nullptr, 0, !accumulate, use_bv != 0);
     } else {
         s = run_trace(c, seg, chunks, pl, nullptr, 0, !accumulate);
     }
@@ -1310,10 +1352,12 @@ rf_status rf_trace_rays(rf_ctx *c, int32_t emitter, int64_t first_ray, int64_t n
     RF_CUDA(c, cudaSetDevice(c->device));
     RF_CUDA(c, c->d_rec.ensure((size_t)n_rays * 4));
     if (c->cfg.precision == RF_PREC_MIXED) {
-        if (use_bv) return fail(c, RF_ERR_UNSUPPORTED, "bounding-surface semantics need EXACT, FAST or FP64");
+        if (use_bv && (s = check_mixed_bv(c)) != RF_OK) return s;
         std::vector<Segment> seg;
-        const int64_t chunks = plan_segments(seg, emitter, 0, first_ray, n_rays, mixed_chunk_draws(c, true), 0);
-        if ((s = run_mixed(c, seg, chunks, true, c->d_rec.as<int32_t>(), first_ray, false)) != RF_OK) return s;
+        const int64_t chunks =
+            plan_segments(seg, emitter, 0, first_ray, n_rays, mixed_chunk_draws(c, true, use_bv != 0), 0);
+        if ((s = run_mixed(c, seg, chunks, true, c->d_rec.as<int32_t>(), first_ray, false, use_bv != 0)) != RF_OK)
+            return s;
     } else {
         Plan pl = make_plan(c, use_bv != 0, true);
         const int64_t chunk_gids = (int64_t)pl.lc.block * pl.lc.gpt;
@@ -1880,10 +1924,8 @@ rf_status rf_autotune(rf_ctx *c, int32_t use_bv, const char *cache_path)
     rf_status s = require_scene(c);
     if (s != RF_OK) return s;
     if (use_bv && c->nbv <= 0) return fail(c, RF_ERR_STATE, "use_bv set but the scene has no bounding volumes");
-    if (c->cfg.precision == RF_PREC_MIXED) {
-        if (use_bv) return fail(c, RF_ERR_UNSUPPORTED, "bounding-surface semantics need EXACT, FAST or FP64");
-        return autotune_mixed(c, cache_path);
-    }
+    if (c->cfg.precision == RF_PREC_MIXED)  // with bounding surfaces: one kernel, nothing to choose
+        return use_bv ? check_mixed_bv(c) : autotune_mixed(c, cache_path);
     const std::string key = tune_key(c, use_bv ? 1 : 0);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);

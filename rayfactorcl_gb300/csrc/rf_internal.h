@@ -118,6 +118,8 @@ template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
 // Batched mixed-precision persistent kernel (rf_kern_fast.cu); count: also
 // collect the work counters (TraceParams::work).
 cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool count, int grid, cudaStream_t st);
+// The same kernel with runBVGPU's bounding-surface semantics (one resident scene).
+cudaError_t launch_batched_bv(const TraceParams &p, bool rec, int grid, cudaStream_t st);
 int batched_blocks_per_sm(bool rec, bool resident);
 cudaError_t launch_build_masks(const MaskInputs &in, uint32_t *out, cudaStream_t st);
 // Mixed-precision kernel for one small scene with the plain kernel's launch shape
@@ -131,6 +133,7 @@ int batched_tile();  // scenes with at most this many surfaces use the resident 
 constexpr int kBatchTile = 512;  // surfaces the resident kernel keeps in shared memory
 constexpr int kBatchBruteMax = 12;  // scenes up to this many surfaces are traced without culling
 constexpr int kEmitFrameWords = 5;  // float4 words of a planar emitter's frame (mixed kernels)
+constexpr int kBatchMaxBV = 16;     // bounding surfaces the mixed kernel takes (runBVGPU semantics)
 constexpr int kBatchMaxSurfaces = 32767;  // nearest hits are kept as int16 in shared memory
 constexpr int kBatchChunkDraws = 8192;  // Philox draws per chunk of the batched kernel
 

@@ -13,11 +13,13 @@ static_assert(kBatchThreads * kBatchDraws == kBatchChunkDraws, "chunk size");
 
 size_t batched_smem_bytes() { return sizeof(BatchSmem); }
 
-template <bool REC, bool RES, bool CNT>
+static_assert(sizeof(BatchSmem) <= 227 * 1024, "the batched kernel's shared memory exceeds a block's 227 KB");
+
+template <bool REC, bool RES, bool CNT, bool BV = false>
 static cudaError_t launch_b(const TraceParams &p, int grid, cudaStream_t st)
 {
     const size_t smem = sizeof(BatchSmem);
-    auto k = batched_kernel<REC, RES, CNT>;
+    auto k = batched_kernel<REC, RES, CNT, BV>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<grid, kBatchThreads, smem, st>>>(p);
@@ -31,12 +33,18 @@ cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool c
     return resident ? launch_b<false, true, false>(p, grid, st) : launch_b<false, false, false>(p, grid, st);
 }
 
+cudaError_t launch_batched_bv(const TraceParams &p, bool rec, int grid, cudaStream_t st)
+{
+    if (p.nbv <= 0 || p.nbv > kBatchMaxBV || p.n > kBatchTile) return cudaErrorInvalidValue;
+    return rec ? launch_b<true, true, false, true>(p, grid, st) : launch_b<false, true, false, true>(p, grid, st);
+}
+
 template <bool REC, bool RES>
 static int occ_b()
 {
     const size_t smem = sizeof(BatchSmem);
     int nb = 0;
-    auto k = batched_kernel<REC, RES, false>;
+    auto k = batched_kernel<REC, RES, false, false>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kBatchThreads, smem);
     return nb;

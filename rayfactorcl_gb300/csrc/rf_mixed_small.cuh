@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kSmallThreads) mixed_small_kernel(const TraceP
         for (int k = 0; k < R; ++k) {
             const int64_t rid = (gid0 + (int64_t)(k >> 2) * blockDim.x + tid) * 4 + (k & 3);
             const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
-            const int h = valid ? resolve_brute(bi[k], tb[k], dj[k], n, true, s_tab, nullptr, s_bs, nullptr, ray[k],
+            const int h = valid ? resolve_brute(bi[k], tb[k], dj[k], 0, n, true, s_tab, nullptr, s_bs, nullptr, ray[k],
                                                 eps, sc, skip, nref)
                                 : -1;
             if (REC) {

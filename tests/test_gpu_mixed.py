@@ -260,7 +260,10 @@ def test_batch_rejects_bad_input(built_lib):
         assert ei.value.status == 2
         with pytest.raises(_lib.RfError):
             t.converge_batch([sc], [np.array([4, 4])], tol=0.0, round_rays=4, max_rounds=2)
-        t.set_scene(golden_scene("input-C52-BV"))
+        # bounding-surface semantics: at most 16 bounding surfaces in the mixed kernel
+        bv = golden_scene("input-C52-BV")
+        many = np.concatenate([bv.bounding_volumes] * 9)  # 18 > 16
+        t.set_scene(type(bv)(1e6, True, bv.primitives, many))
         with pytest.raises(_lib.RfError) as ei:
             t.trace([4, 4], use_bv=True)
         assert ei.value.status == 8
@@ -338,3 +341,50 @@ def test_mixed_autotune_keeps_results(built_lib):
         t.autotune()
         h1, _ = t.trace(rays)
     assert np.array_equal(h0, h1)
+
+
+@pytest.mark.parametrize("compat", [0, "all"])
+@pytest.mark.parametrize("name", ["input-C14-BV", "input-C52-BV", "gen_furnace"])
+def test_mixed_bounding_surfaces_per_ray(built_lib, oracle_lib, name, compat):
+    """runBVGPU semantics (RayFactorGPU.cl:580-619) in the mixed kernel: per-ray hits
+    against the FP32 and FP64 restatements of the bounding-surface walk, with and
+    without the reference's quirks (stale child index, sphere discriminant, shared
+    streams)."""
+    from rayfactorcl_gb300 import _lib
+    cpt = _lib.COMPAT_ALL if compat == "all" else 0
+    sc = golden_scene(name)
+    p = O.params(compat=cpt, use_bv=True)
+    total = bad = 0
+    emitters = sorted(set([0, sc.n // 3, sc.n // 2, sc.n - 1]))
+    with _tracer(sc, precision=PREC_MIXED, compat=cpt) as t:
+        for e in emitters:
+            got = t.trace_rays(e, 3, 8192, use_bv=True)
+            e64 = O.trace_rays(sc, p, e, 3, 8195, f64=True)
+            e32 = O.trace_rays(sc, p, e, 3, 8195)
+            total += got.size
+            bad += int(np.count_nonzero((got != e64) & (got != e32)))
+            assert (got >= 0).mean() > 0.05
+    assert bad / total <= 2e-3, (bad, total)
+
+
+def test_mixed_bounding_surfaces_tallies(built_lib):
+    """Tallies of the mixed kernel with bounding surfaces against the exact kernel's
+    runBVGPU on the same streams: apart from the rows of planar emitters facing -z
+    (where FP32 and FP64 frames trace different, equally valid rays; module
+    docstring), rays that differ are grazing ones; every row agrees to well within
+    its binomial sigma."""
+    sc = golden_scene("gen_furnace")
+    rays = np.full(sc.n, 20_000, np.int64)
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        hm, Fm = t.trace(rays, use_bv=True)
+    with _tracer(sc, precision=PREC_EXACT) as t:
+        he, Fe = t.trace(rays, use_bv=True)
+    keep = np.array([not faces_minus_z(sc.primitives[e]) for e in range(sc.n)])
+    assert keep.sum() > sc.n // 2
+    diff = np.abs(hm.astype(np.int64) - he.astype(np.int64))[keep]
+    assert int(diff.sum()) <= 2e-3 * 2 * rays[keep].sum()
+    # sigma of the difference of two estimates of the same F (independent rays on
+    # the -z rows), with a floor of one hit for cells neither run saw often
+    Fbar = 0.5 * (Fm + Fe)
+    sig = np.sqrt(2 * np.maximum(Fbar * (1 - Fbar), 1.0 / rays[:, None]) / rays[:, None])
+    assert float(np.max(np.abs(Fm - Fe) / sig)) < 5
