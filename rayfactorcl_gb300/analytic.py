@@ -67,3 +67,67 @@ def enclosure3(r: float = 0.5, h: float = 1.0) -> np.ndarray:
 
 def areas_of(ws_areas) -> np.ndarray:
     return np.asarray(ws_areas, np.float64)
+
+
+def concentric_cylinders(r1: float, r2: float, l: float) -> float:
+    """Inner surface of a cylinder of radius r2 to the outer surface of a coaxial
+    cylinder of radius r1 < r2, both of length l with common ends (F_21)."""
+    R, L = r2 / r1, l / r1
+    A = L * L + R * R - 1.0
+    B = L * L - R * R + 1.0
+    inner = (math.sqrt((A + 2.0) ** 2 - (2.0 * R) ** 2) * math.acos(B / (R * A))
+             + B * math.asin(1.0 / R) - 0.5 * math.pi * A)
+    return 1.0 / R - (math.acos(B / A) - inner / (2.0 * L)) / (math.pi * R)
+
+
+def concentric_cylinders_quadrature(r1: float, r2: float, l: float) -> float:
+    """The same view factor by FP64 quadrature of the double-area integral.  With
+    the outer point at angle 0 and the inner one at angle phi, both axial integrals
+    have closed forms (int int dz1 dz2 / (q + (z1-z2)^2)^2 over [0,l]^2), leaving one
+    integral over |phi| < acos(r1/r2), where the inner surface faces the outer point."""
+    from scipy.integrate import quad
+
+    def axial(q):
+        rq = math.sqrt(q)
+        j1 = l / (2 * q * (q + l * l)) + math.atan(l / rq) / (2 * q * rq)
+        j2 = 1 / (2 * q) - 1 / (2 * (q + l * l))
+        return 2 * (l * j1 - j2)
+
+    def f(phi):
+        c = math.cos(phi)
+        q = r1 * r1 + r2 * r2 - 2 * r1 * r2 * c
+        return (r2 - r1 * c) * (r2 * c - r1) * axial(q)
+
+    p0 = math.acos(r1 / r2)
+    val, _ = quad(f, -p0, p0, epsabs=1e-14, epsrel=1e-12, limit=200)
+    return r1 * val / (math.pi * l)
+
+
+def cylinder_to_base_annulus_quadrature(r1: float, l: float, r2: float) -> float:
+    """Outer surface of a cylinder (radius r1, length l) to the annulus r1 <= rho <= r2
+    around its base, in the base plane and facing the cylinder's side (the
+    sample geometry input-C77.xml).  The double-area integral with the cylinder
+    point at angle 0: the axial integral int_0^l z dz / (q + z^2)^2 and the
+    angular one over |phi| < acos(r1/rho) (where the annulus point lies in front
+    of the cylinder surface; int dphi / (a - b cos phi) by the half-angle
+    tangent) are closed forms, leaving one FP64 quadrature over rho.  The
+    cylinder is convex and the annulus flat, so nothing blocks the lines."""
+    from scipy.integrate import quad
+
+    def g(rho, dm, a):  # int_{-p0}^{p0} (rho cos phi - r1) / (a - b cos phi) dphi, b = 2 rho r1, dm = a - b
+        b = 2 * rho * r1
+        p0 = math.acos(min(1.0, r1 / rho))
+        root = math.sqrt(dm * (a + b))
+        return -(rho / b) * 2 * p0 + (rho * a / b - r1) * 4 / root * math.atan(
+            math.sqrt((a + b) / dm) * math.tan(0.5 * p0))
+
+    def f(t):  # rho = r1 + t^2 spreads the edge's square-root behaviour
+        rho = r1 + t * t
+        if t == 0.0:
+            return 0.0
+        e2 = (rho - r1) ** 2  # a - b without cancellation
+        a0 = rho * rho + r1 * r1
+        return 2 * t * rho * 0.5 * (g(rho, e2, a0) - g(rho, e2 + l * l, a0 + l * l))
+
+    val, _ = quad(f, 0.0, math.sqrt(r2 - r1), epsabs=1e-14, epsrel=1e-12, limit=400)
+    return val / (math.pi * l)

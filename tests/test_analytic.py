@@ -214,3 +214,46 @@ def test_oracle_bv_stale_quirk(oracle_lib):
     # near-horizontal rays that miss the upper disc's rim reach the lower one
     assert stale[1, 0] > 0.99 * rays[1] and stale[1, 2] < 0.01 * rays[1]
     assert fixed[1, 2] > 0.99 * rays[1] and fixed[1, 0] == 0      # the nearer plain BV wins
+
+
+@pytest.mark.parametrize("r1,r2,l", [(0.5, 1.0, 1.0), (1.0, 2.0, 0.5), (1.0, 1.5, 4.0), (0.2, 1.0, 2.0)])
+def test_concentric_cylinders(r1, r2, l):
+    """Outer cylinder's inside to the inner cylinder: closed form vs FP64 quadrature."""
+    assert abs(analytic.concentric_cylinders(r1, r2, l) - analytic.concentric_cylinders_quadrature(r1, r2, l)) < 1e-10
+
+
+def _c77_dblquad(r1, l, r2):
+    """Independent check of the reduced form: 2-D quadrature over (rho, phi) with only
+    the axial integral done in closed form."""
+    from scipy.integrate import dblquad
+
+    def f(phi, rho):
+        q = rho * rho + r1 * r1 - 2 * rho * r1 * math.cos(phi)
+        return rho * (rho * math.cos(phi) - r1) * (0.5 / q - 0.5 / (q + l * l))
+
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        val, _ = dblquad(f, r1, r2, lambda rho: -math.acos(r1 / rho), lambda rho: math.acos(r1 / rho),
+                         epsabs=1e-12, epsrel=1e-10)
+    return val / (math.pi * l)
+
+
+@pytest.mark.parametrize("r1,l,r2", [(2.0, 1.0, 3.0), (1.0, 2.0, 1.5)])
+def test_cylinder_to_base_annulus(r1, l, r2):
+    """input-C77.xml's pair: the 1-D reduced quadrature against a 2-D quadrature of
+    the same integral."""
+    ref = analytic.cylinder_to_base_annulus_quadrature(r1, l, r2)
+    assert abs(ref - _c77_dblquad(r1, l, r2)) < 1e-7
+
+
+def test_oracle_C77_cylinder_to_annulus(oracle_lib):
+    """The sample geometry itself traced by the oracle's FP64 tracer (absolute eps
+    1e-6 instead of the reference's 1e-3, which drops hits where the annulus meets
+    the cylinder) against the quadrature."""
+    sc = golden_scene("input-C77")
+    n = 4_000_000
+    rows = O.tally(sc, O.params(compat=0, eps=1e-6), np.array([n, 0]), f64=True)
+    ref = analytic.cylinder_to_base_annulus_quadrature(2.0, 1.0, 3.0)
+    sigma = math.sqrt(ref * (1 - ref) / n)
+    assert abs(rows[0, 1] / n - ref) < 5 * sigma
