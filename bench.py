@@ -39,6 +39,7 @@ sys.path.insert(0, str(ROOT))
 # FP32 operations per call from the source of RayFactorGPU.cl (FMA/mad = 1, MUFU not counted).
 TEST_OPS = {0: 33, 1: 39, 2: 33, 3: 23, 4: 21, 5: 23}      # per ray x surface test, by type
 EMIT_OPS = {0: 52, 1: 58, 2: 55, 3: 52, 4: 48, 5: 50}      # per emitted ray, by emitter type
+SPHERE_CHECK_OPS = 12                                          # per ray x bounding-sphere check
 METRIC = "rays/s on 1 GB300: batched mixed-precision vs plain kernel at equal F error"
 
 
@@ -126,6 +127,16 @@ WORKLOADS = {
 }
 
 
+def workload_label(args) -> str:
+    if args.workload in WORKLOADS:
+        return WORKLOADS[args.workload]
+    if args.surfaces == 64:
+        return ("mixed64 seed 2: 64 surfaces (16 cyl, 16 frustum, 12 disc, 10 annulus, 10 sphere), "
+                "1e8 rays/step spread by area")
+    return (f"mixed scene seed 2: {args.surfaces} surfaces (mixed64 type mix), {args.rays:.0e} rays/step "
+            "spread by area")
+
+
 def workload(args):
     from rayfactorcl_gb300 import generators
     if args.workload == "enclosure3":
@@ -174,31 +185,41 @@ def cpu_rate(w, seconds: float, threads: int = 0):
     O.tally(w.scene, p, sample, threads=threads)
     dt = time.perf_counter() - t0
     nthreads = threads if threads > 0 else O.max_threads()
-    return float(sample.sum()) / dt, int(sample.sum()), nthreads, dt
+    return float(sample.sum()) / dt, sample, nthreads, dt
 
 
 def run_reference(args):
+    """The reference method on the host cores: the CPU restatement of runGPU
+    (RayFactorGPU.cl:481-527) with OpenMP over all cores.  Every step traces the
+    same bounded, area-weighted sample of the workload (sized once, about
+    --ref-seconds of CPU work), timed on its own; value = sample rays / mean step
+    time.  Under torchrun only rank 0 works."""
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
     w = workload(args)
     from oracle import oracle as O
     O.lib()
-    rates = []
-    sample_rays = 0
+    _, sample, nthreads, _ = cpu_rate(w, seconds=args.ref_seconds)
+    p = O.params(compat=0, key1=w.key1)
+    step_s = []
     for i in range(args.warmup + args.steps):
-        rate, sample_rays, nthreads, _ = cpu_rate(w, seconds=args.ref_seconds)
+        t0 = time.perf_counter()
+        O.tally(w.scene, p, sample)
         if i >= args.warmup:
-            rates.append(rate)
-    value = float(np.mean(rates))
+            step_s.append(time.perf_counter() - t0)
+    rays = int(sample.sum())
+    value = rays / float(np.mean(step_s))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.rays / value,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(step_s)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": "mixed64 seed 2, 64 surfaces, 1e8 rays/step",
-                                        "kernel": "CPU restatement of RayFactorGPU.cl runGPU"},
+        "data": "synthetic", "config": {"workload": workload_label(args),
+                                        "kernel": "CPU restatement of RayFactorGPU.cl runGPU",
+                                        "rays_per_step": rays,
+                                        "step": f"a {rays}-ray area-weighted sample of the workload"},
         "cpu_baseline": {"value": value, "unit": "rays/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{sample_rays} rays of the workload per step, area-weighted"},
+                         "sample": f"{rays} rays of the workload per step, area-weighted"},
         "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -226,6 +247,46 @@ def time_trace(t, rays, steps, warmup, l2_flush, stream, use_bv=False):
         step_ms.append(e0.elapsed_time(e1))
         kern_ms.append(t.last_stats()[0])
     return float(np.mean(step_ms)), float(np.mean(kern_ms))
+
+
+def time_sharded(t, rays, rank, world, steps, warmup, dev, use_bv, l2_flush, with_upload=None):
+    """N ranks, weak scaling: rank r traces its share of a run of world x rays per
+    emitter (ray ranges split on Philox draws, rayfactorcl_gb300.shard), reads its
+    int64 tallies and joins one all_reduce of them -- the path's only exchange
+    step (the reference sums per-device tallies on the host, main.cpp:224-234).
+    Wall time per step, max over ranks; with_upload(): re-upload the scene first
+    (the end-to-end variant)."""
+    import torch
+    import torch.distributed as dist
+
+    from rayfactorcl_gb300 import shard
+    first, count = shard.shard_ranges(np.asarray(rays, np.int64) * world, rank, world)
+    n = len(rays)
+    hits = np.zeros((n, n), np.uint64)
+    out = torch.zeros(n * n, dtype=torch.int64, device=dev)
+
+    def step():
+        if with_upload is not None:
+            with_upload()
+        t.trace_range(first, count, use_bv)
+        t.read_results(hits, None)
+        out.copy_(torch.from_numpy(hits.view(np.int64).reshape(-1)))
+        dist.all_reduce(out, op=dist.ReduceOp.SUM)
+
+    for _ in range(warmup):
+        step()
+    total = 0.0
+    for _ in range(steps):
+        l2_flush.zero_()
+        torch.cuda.synchronize()
+        dist.barrier()
+        t0 = time.perf_counter()
+        step()
+        torch.cuda.synchronize()
+        total += time.perf_counter() - t0
+    m = torch.tensor([1e3 * total / steps], device=dev)
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    return float(m.item()), t.last_stats()[0]
 
 
 def run_ours(args):
@@ -264,27 +325,32 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
-    def tracer(prec):
-        t = Tracer(precision=prec, key1=w.key1, device=local, rays_per_thread=args.rays_per_thread)
+    def tracer(prec, tally_mode=0):
+        t = Tracer(precision=prec, key1=w.key1, device=local, rays_per_thread=args.rays_per_thread,
+                   tally_mode=tally_mode)
         t.set_scene(sc)
         return t, torch.cuda.ExternalStream(t.stream_handle, device=dev)
 
     # -- headline kernel: scene resident, per-step device time ------------
-    t, stream = tracer(headline)
+    t, stream = tracer(headline, args.tally_mode)
     head_bv = plain_bv
     # launch shape (plain kernels) or kernel choice (mixed: small-scene vs batched) for these budgets
     t.trace_async(rays, head_bv)
     t.read_results(None, None)
-    t.autotune(head_bv)
+    if not args.tally_mode:  # a fixed tally mode is measured as chosen
+        t.autotune(head_bv)
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        ms_step, kernel_ms = time_trace(t, rays, args.steps, args.warmup, l2_flush, stream, head_bv)
+        if world > 1:  # sharded ray ranges + one tally sum
+            ms_step, kernel_ms = time_sharded(t, rays, rank, world, args.steps, args.warmup, dev, head_bv, l2_flush)
+        else:
+            ms_step, kernel_ms = time_trace(t, rays, args.steps, args.warmup, l2_flush, stream, head_bv)
         torch.cuda.synchronize()
     barrier()
     hits = np.zeros((sc.n, sc.n), np.uint64)
     t.read_results(hits, None)
-    assert int(hits.sum()) <= total_rays
+    assert int(hits.sum()) <= total_rays * world
     refined = t.refined_count() if headline == PREC_MIXED else 0
     work = None
     if headline == PREC_MIXED:  # the timed kernel does not count; one more run that does
@@ -292,26 +358,27 @@ def run_ours(args):
             tc.set_scene(sc)
             tc.trace(rays, head_bv)
             work = tc.work_counts()
-    if world > 1:
-        import torch.distributed as dist
-        m = torch.tensor([ms_step], device=dev)
-        dist.all_reduce(m, op=dist.ReduceOp.MAX)
-        ms_step = float(m.item())
     value = world * total_rays / (ms_step * 1e-3)
 
     # -- e2e: host buffers through the C ABI (scene upload, trace, FP64 F, read-back)
     e2e_ms = []
-    for i in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        t.set_scene(sc)
-        t.trace(rays, head_bv)
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_ms = e2e_ms[args.warmup:]
+    if world > 1:  # the sharded step with the scene uploaded each time
+        e2e_ms.append(time_sharded(t, rays, rank, world, args.steps, args.warmup, dev, head_bv, l2_flush,
+                                   with_upload=lambda: t.set_scene(sc))[0])
+    else:
+        for i in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            t.set_scene(sc)
+            t.trace(rays, head_bv)
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e_ms = e2e_ms[args.warmup:]
     h2d = sc.primitives.nbytes + sc.n * 64 + rays.nbytes + 32 * sc.n + 8 * sc.n
     if headline == PREC_MIXED:
-        h2d += sc.n * (112 + 64 + 16)
-    d2h = sc.n * sc.n * 16
+        # re-centred records, hit records, spheres, patch balls, sphere chains, planes,
+        # emission frames, mask rows and offsets; the cones of the direction cells
+        h2d += sc.n * (112 + 64 + 16 + 16 * 16 + 8 * 16 + 16 + 5 * 16 + 8 + 16) + 512 * 16
+    d2h = sc.n * sc.n * (16 if world == 1 else 8)
     t.close()
 
     # roofline of the headline kernel: FP32 work it performed / its time
@@ -319,8 +386,11 @@ def run_ours(args):
         types = sc.primitives["type"].astype(int)
         emit = float(sum(int(r) * EMIT_OPS[int(ty)] for r, ty in zip(rays, types)))
         tests = float(sum(int(work[k]) * TEST_OPS[k] for k in range(6)))
-        cone = 20.0 * float(work[6])
-        done_ops = emit + tests + cone
+        # every candidate of a packet gets a ray/bounding-sphere check in each of the
+        # 32 lanes (12 FP32 operations: three differences, two dot products, the
+        # clamp, the closest-approach product and its fma)
+        checks = SPHERE_CHECK_OPS * 32.0 * float(work[6])
+        done_ops = emit + tests + checks
         all_pairs = float(total_rays) * sc.n
         culled = 1.0 - float(sum(int(work[k]) for k in range(6))) / all_pairs
     else:
@@ -393,20 +463,25 @@ def run_ours(args):
     # -- CPU baseline -----------------------------------------------------
     cpu = None
     if rank == 0 and not args.no_cpu:
-        rate, sample_rays, nthreads, dt = cpu_rate(w, seconds=args.cpu_seconds)
+        rate, sample, nthreads, dt = cpu_rate(w, seconds=args.cpu_seconds)
+        rate1, sample1, _, dt1 = cpu_rate(w, seconds=args.cpu_seconds / 3, threads=1)
         cpu = {"value": rate, "unit": "rays/s", "cores": nthreads, "kind": "port",
-               "sample": f"{sample_rays} rays of the workload, area-weighted, {dt:.1f} s"}
+               "sample": f"{int(sample.sum())} rays of the workload, area-weighted, {dt:.1f} s",
+               "single_thread": {"value": rate1, "unit": "rays/s", "cores": 1,
+                                 "sample": f"{int(sample1.sum())} rays of the workload, area-weighted, {dt1:.1f} s"}}
 
     hbm_peak = None
     try:
         hbm_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
     except (OSError, ValueError, KeyError):
         hbm_peak = None
+    # DRAM bytes per launch of the timed kernel from an ncu capture of this workload
+    # (profiles/traffic.json, key "<workload>:<precision>"); null when none was made
     traffic = None
     prof = ROOT / "profiles" / "traffic.json"
-    if prof.exists():
+    if prof.exists() and args.surfaces == 64 and args.rays == 100_000_000:
         try:
-            traffic = json.loads(prof.read_text()).get(f"{args.precision}_bytes_per_launch")
+            traffic = json.loads(prof.read_text()).get(f"{args.workload}:{args.precision}")
         except (ValueError, OSError):
             traffic = None
 
@@ -417,12 +492,12 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload] if args.workload in WORKLOADS else ("mixed64 seed 2: 64 surfaces (16 cyl, 16 frustum, 12 disc, 10 annulus, "
-                                "10 sphere), 1e8 rays/step spread by area") if args.surfaces == 64 else
-                               f"mixed scene seed 2: {args.surfaces} surfaces (mixed64 type mix), "
-                               f"{args.rays:.0e} rays/step spread by area",
+        "config": {"workload": workload_label(args),
                    "kernel": kname, "l2": "flushed between steps (256 MB write)",
-                   "rays_per_step": total_rays},
+                   "rays_per_step": total_rays * world,
+                   "parallelism": ("one GPU" if world == 1 else
+                                   f"{world} GPUs: ray ranges of each emitter's stream split on Philox draws, "
+                                   "one int64 all_reduce of the tallies per step")},
         "e2e": {"value": world * total_rays / (float(np.mean(e2e_ms)) * 1e-3), "unit": "rays/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "fp32-issue", "achieved": achieved / 1e12, "peak": peak_ops / 1e12,
@@ -537,8 +612,11 @@ def main():
     ap.add_argument("--rays", type=int, default=100_000_000)
     ap.add_argument("--surfaces", type=int, default=64, help="surfaces of the mixed scene (same type mix)")
     ap.add_argument("--rays-per-thread", type=int, default=0, choices=[0, 4, 8])
+    ap.add_argument("--tally-mode", type=int, default=0, choices=[0, 1, 2],
+                    help="plain headline kernel: 1 shared-memory row histogram, 2 global atomics per ray "
+                         "(as runGPU's atomic_inc, RayFactorGPU.cl:524); 0 autotuned")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="mixed64", choices=["mixed64", "sweep", *WORKLOADS])
     ap.add_argument("--sweep-scenes", type=int, default=256)
