@@ -264,11 +264,16 @@ rf_status rf_smooth_F(rf_ctx *ctx, const double *F, const double *areas, int32_t
  * atomics) and test order (a thread's rays together per surface, or one ray
  * at a time); the choice is cached per scene shape in memory and, when cache_path
  * is not NULL, appended to that file and read back by later processes.  Applies
- * the choice to the context.  A no-op for RF_PREC_MIXED (one launch shape).
+ * the choice to the context.  RF_PREC_MIXED: for one scene of at most 64 surfaces, the choice
+ * between the batched kernel and the small-scene kernel with 4 or 8 rays per thread (cached
+ * the same way); with use_bv, a check that the scene fits the bounding-surface variant.
  * Results of a trace do not depend on the launch shape. */
 rf_status rf_autotune(rf_ctx *ctx, int32_t use_bv, const char *cache_path);
 
-/* (No counterpart in the reference.)  The launch shape the context uses now (after rf_autotune, or the defaults). */
+/* (No counterpart in the reference.)  The launch shape the context uses now (after rf_autotune, or the defaults).
+ * RF_PREC_MIXED: the kernel the next trace of the current scene without bounding surfaces takes -- block
+ * 1024 and 32 rays per thread for the batched kernel, 256 and 4 or 8 for the small-scene kernel (with
+ * bounding surfaces it is always the batched kernel). */
 rf_status rf_get_launch_config(rf_ctx *ctx, int32_t *block, int32_t *rays_per_thread,
                                int32_t *smem_hist, int32_t *smem_table, int32_t *one_ray_at_a_time);
 
@@ -277,7 +282,8 @@ rf_status rf_last_refine_count(rf_ctx *ctx, uint64_t *refined_tests);
 
 /* (No counterpart in the reference.)  Work of the last mixed-precision run made with
  * rf_config.work_counts = 1 (zeros otherwise): counts[0..5] ray x surface tests
- * performed by surface type (RF_CYLINDER..RF_DISC), counts[6] candidate
+ * performed by surface type (RF_CYLINDER..RF_DISC; with bounding surfaces, the
+ * tests of their children: each ray also tests every bounding surface), counts[6] candidate
  * surfaces of the packets (the union of their rays' cell masks, or the surfaces
  * their bounds can reach; each then checked ray by ray), counts[7] ray packets
  * (32 rays).  Tests skipped by culling are the all-pairs count minus the sum of

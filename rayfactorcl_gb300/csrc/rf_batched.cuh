@@ -77,11 +77,58 @@ struct BatchSmem {
     HitRec bvtab[kBatchMaxBV];          // bounding surfaces (runBVGPU semantics)
     int4 bvinfo[kBatchMaxBV];           // (settings, first child, end of children, 0)
     int64_t chunk;
+    unsigned long long bar;             // mbarrier of the bulk copies of the scene tables
     int next_packet;
     int n_valid;
     unsigned long long work[8];
     uint32_t wcount[kBatchThreads / 32][8];  // per warp: tests by type, candidates, packets (COUNT)
 };
+
+// Bulk copies (cp.async.bulk: the TMA unit's untiled global -> shared form) of a
+// scene's tables into shared memory, completing on an mbarrier.  Source and
+// destination 16-byte aligned, sizes multiples of 16 (HitRec 64 B, float4 16 B).
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void bar_init(unsigned long long *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One thread: announce `bytes` of transfers on the barrier, then issue them.
+__device__ __forceinline__ void bar_expect(unsigned long long *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Wait for the barrier's phase `parity` to complete; gives up after about 2^31
+// clocks (about a second) and returns false.
+__device__ __forceinline__ bool bar_wait(unsigned long long *bar, uint32_t parity)
+{
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > (1ll << 31)) return false;
+    }
+}
 
 // The top 24 bits of the four Philox words of a draw in three words, and back
 // as the four uniforms of u01_closed_open_4x32_24 (RayFactorGPU.cl:59-62).
@@ -396,46 +443,44 @@ __device__ __forceinline__ bool own_gate(const uint32_t *mcell, int j, const Ray
     return ray_may_hit(ray, idd, b);
 }
 
-// Full nearest-hit search for one ray over the surfaces its gate admits, with
-// FP64 for every ill-conditioned quadric (cold path: the ray deferred more than
-// one test, and a lane keeps only one).
+// Full nearest-hit search for one ray over the surfaces [lo, hi) its gate admits
+// (gated: the cell mask when mcell is set, and the bounding-sphere check; else
+// every surface but skip), with FP64 for every ill-conditioned quadric; nf64
+// counts the FP64 evaluations.  Cold path: rays that deferred a test they could
+// not resolve in their hot loop.
 __device__ __noinline__ int retrace_f64(int lo, int hi, bool resident, const HitRec *stab, const HitRec *gtab,
-                                        const float4 *sbs, const float4 *gbs, const uint32_t *mcell,
-                                        const Ray<float> &ray, float idd, float eps, bool sc, int skip)
+                                        const float4 *sbs, const float4 *gbs, const uint32_t *mcell, bool gated,
+                                        const Ray<float> &ray, float idd, float eps, bool sc, int skip, int &nf64)
 {
     float tb = MFast::inf();
     int bi = -1;
     for (int j = lo; j < hi; ++j) {
-        if (j == skip || !own_gate(mcell, j, ray, idd, resident ? sbs[j] : __ldg(gbs + j))) continue;
+        if (j == skip) continue;
+        if (gated && !own_gate(mcell, j, ray, idd, resident ? sbs[j] : __ldg(gbs + j))) continue;
         const HitRec h = resident ? stab[j] : load_rec(gtab, j);
         bool defer = false;
         float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
-        if (defer) t = hit_f64(h, ray, eps, sc);
+        if (defer) {
+            t = hit_f64(h, ray, eps, sc);
+            ++nf64;
+        }
         if (t < tb) { tb = t; bi = j; }
     }
     return bi;
 }
 
-// Nearest hit of a ray tested against all surfaces [lo, hi): bi / tb from the index-order
-// loop, dj the deferred test (-1 none, j the only one, -2 several).  One deferral
-// is re-evaluated in FP64 (lower index wins a tie: it ran out of order); several
-// re-trace the ray with FP64 for each.  Shared by the small-scene paths of the
-// batched kernel and of mixed_small_kernel, so both give the same result.
-__device__ __forceinline__ int resolve_brute(int bi, float tb, int dj, int lo, int hi, bool resident,
-                                             const HitRec *stab, const HitRec *gtab, const float4 *sbs,
-                                             const float4 *gbs, const Ray<float> &ray, float eps, bool sc, int skip,
-                                             int &nref)
+// Nearest hit of a ray tested against every surface of [lo, hi) but skip, in
+// index order: bi from the hot loop, deferred whether it deferred any test; such
+// a ray is traced again with FP64 for each deferred test.  Shared by the
+// small-scene paths of the batched kernel and of mixed_small_kernel, so both
+// give the same result.
+__device__ __forceinline__ int resolve_brute(int bi, bool deferred, int lo, int hi, bool resident,
+                                             const HitRec *stab, const HitRec *gtab, const Ray<float> &ray,
+                                             float eps, bool sc, int skip, int &nref)
 {
-    if (dj >= 0) {
-        const HitRec hq = resident ? stab[dj] : load_rec(gtab, dj);
-        const float t = hit_f64(hq, ray, eps, sc);
-        if (t < tb || (t == tb && bi >= 0 && dj < bi)) bi = dj;
-        ++nref;
-    } else if (dj == -2) {
-        bi = retrace_f64(lo, hi, resident, stab, gtab, sbs, gbs, nullptr, ray,
-                         MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz), eps, sc, skip);
-        nref += 2;
-    }
+    if (deferred)
+        bi = retrace_f64(lo, hi, resident, stab, gtab, nullptr, nullptr, nullptr, false, ray, 0.0f, eps, sc, skip,
+                         nref);
     return bi;
 }
 
@@ -503,6 +548,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
     int row_chunks = 0;   // chunks tallied into the shared-memory row since its last flush
     uint32_t tcount = 0;  // COUNT, lane t < 6: lane-tests of surfaces of type t by this warp (this chunk)
     const uint32_t *mrow = nullptr;  // cell masks of the current row (null: packet bounds instead)
+    uint32_t bar_parity = 0;         // phase of S.bar the next table copy completes
+    if (RESIDENT && tid == 0) bar_init(&S.bar);  // visible after the chunk loop's first barrier
 
     auto flush = [&]() {
         __syncthreads();
@@ -543,6 +590,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
             flush();                                     // (at most 32768 hits per bin per chunk)
             row_chunks = 0;
         }
+        bool staged = false;  // RESIDENT: this chunk copies a new scene's tables
         if (sg.scene != cur_scene || sg.emitter != cur_emitter) {
             if (!REC) flush();
             row_chunks = 0;
@@ -552,11 +600,16 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 hist_on = !REC && si.n <= kBatchHist;
                 if (hist_on)
                     for (int i = tid; i < si.n; i += blockDim.x) S.hist[i] = 0;
-                if (RESIDENT) {  // resident tables
-                    const float4 *src = reinterpret_cast<const float4 *>(p.tab + si.prim_off);
-                    float4 *dst = reinterpret_cast<float4 *>(S.tab);
-                    for (int i = tid; i < 4 * si.n; i += blockDim.x) dst[i] = __ldg(src + i);
-                    for (int i = tid; i < si.n; i += blockDim.x) S.bs[i] = __ldg(p.bsph + si.prim_off + i);
+                if (RESIDENT) {  // resident tables: two bulk copies, waited for below
+                    // (every thread finished with the previous tables before the chunk's barrier)
+                    if (tid == 0) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        const uint32_t tb = (uint32_t)(sizeof(HitRec) * si.n), sb = (uint32_t)(sizeof(float4) * si.n);
+                        bar_expect(&S.bar, tb + sb);
+                        bulk_load(S.tab, p.tab + si.prim_off, tb, &S.bar);
+                        bulk_load(S.bs, p.bsph + si.prim_off, sb, &S.bar);
+                    }
+                    staged = true;
                 }
                 if (BV) {
                     for (int i = tid; i < 4 * p.nbv; i += blockDim.x)
@@ -575,6 +628,15 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 const int64_t mo = p.mask_off[si.prim_off + sg.emitter];
                 if (mo >= 0) mrow = p.cmask + mo;
             }
+        }
+        if (RESIDENT && staged) {  // block-uniform: every thread waits for the copies
+            const bool ok = bar_wait(&S.bar, bar_parity);
+            if (__syncthreads_or(!ok)) {  // gave up: flag it, let the copies land (bounded), stop
+                if (!ok) bar_wait(&S.bar, bar_parity);
+                if (tid == 0 && p.err) atomicExch(p.err, 3);
+                return;
+            }
+            bar_parity ^= 1u;
         }
         for (int i = tid; i < kCells; i += blockDim.x) S.cnt[i] = 0;
         if (tid == 0) S.next_packet = 0;
@@ -607,17 +669,17 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         const Ray<float> ray = emit_mixed(S.emit, S.frame, r);
                         auto find = [&](int lo, int hi) {  // every child of [lo, hi), index order
                             float tr = MFast::inf();
-                            int br = -1, dr = -1;
+                            int br = -1;
+                            bool dr = false;
                             for (int j = lo; j < hi; ++j) {
                                 if (j == skip) continue;
                                 const HitRec h = S.tab[j];
                                 bool defer = false;
                                 const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
                                 if (t < tr) { tr = t; br = j; }
-                                dr = defer ? (dr == -1 ? j : -2) : dr;
+                                dr |= defer;
                             }
-                            return resolve_brute(br, tr, dr, lo, hi, true, S.tab, gtab, S.bs, p.bsph + si.prim_off, ray,
-                                                 eps, sc, skip, nref);
+                            return resolve_brute(br, dr, lo, hi, true, S.tab, gtab, ray, eps, sc, skip, nref);
                         };
                         bi = bv_select(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0, find);
                     } else if (valid) {
@@ -626,7 +688,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         for (int i = 0; i < 4; ++i) r[i] = uf[(i + v + 1) & 3];
                         const Ray<float> ray = emit_mixed(S.emit, S.frame, r);
                         float tb = MFast::inf();
-                        int dj = -1;
+                        bool dany = false;
 #pragma unroll 1
                         for (int j = 0; j < si.n; ++j) {
                             if (j == skip) continue;  // uniform: every thread's emitter
@@ -634,10 +696,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             bool defer = false;
                             const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
                             if (t < tb) { tb = t; bi = j; }
-                            dj = defer ? (dj == -1 ? j : -2) : dj;
+                            dany |= defer;
                         }
-                        bi = resolve_brute(bi, tb, dj, 0, si.n, RESIDENT, S.tab, gtab, S.bs, p.bsph + si.prim_off,
-                                           ray, eps, sc, skip, nref);
+                        bi = resolve_brute(bi, dany, 0, si.n, RESIDENT, S.tab, gtab, ray, eps, sc, skip, nref);
                     }
                     // all 32 lanes reach the warp-wide calls below
                     if (COUNT) nv_warp += __popc(__ballot_sync(0xffffffffu, valid));
@@ -653,6 +714,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
             if (COUNT) {
                 if (lane == 0 && nv_warp)
                     for (int j = 0; j < si.n; ++j) {
+                        if (j == skip) continue;
                         const int type = RESIDENT ? __float_as_int(S.tab[j].aux.x) : __float_as_int(__ldg(&gtab[j].aux.x));
                         if ((unsigned)type < 6u) S.wcount[warp][type] += nv_warp;
                     }
@@ -775,6 +837,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     // runBVGPU: the nearest child in each bounding surface's range with the
                     // packet's culled candidate loop restricted to the range, then the walk
                     const int skip = self_skip(S.emit, cur_emitter);
+                    if (COUNT && lane == 0) S.wcount[warp][7] += 1;
                     unsigned cmask = 0u;  // without masks: lane w holds candidate word w (n <= kBatchTile)
                     if (!mcell) {
                         const Packet pk = packet_bounds(ray, idd);
@@ -797,13 +860,16 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             if (lo > jw) cm &= ~0u << (lo - jw);
                             if (hi < jw + 32) cm &= (1u << (hi - jw)) - 1u;
                             if (skip >= jw && skip < jw + 32) cm &= ~(1u << (skip - jw));
+                            if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
                             while (cm) {
                                 const int j = jw + __ffs(cm) - 1;
                                 cm &= cm - 1;
                                 if (!__any_sync(0xffffffffu, ray_may_hit(ray, idd, S.bs[j]))) continue;
                                 const HitRec h = S.tab[j];
+                                const int type = __float_as_int(h.aux.x);
+                                if (COUNT) tcount += lane == type ? nvalid : 0;
                                 bool defer = false;
-                                const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
+                                const float t = hit_mixed(type, h, ray, eps, sc, defer);
                                 if (t < tr) { tr = t; br = j; }
                                 nd += defer;
                                 dr = defer ? j : dr;
@@ -819,8 +885,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         }
                         if (valid && !again && br >= 0) again = !own_gate(mcell, br, ray, idd, S.bs[br]);
                         if (again) {
-                            br = retrace_f64(lo, hi, true, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc, skip);
-                            nref += 2;
+                            br = retrace_f64(lo, hi, true, S.tab, gtab, S.bs, gbs, mcell, true, ray, idd, eps, sc, skip,
+                                             nref);
                         }
                         return br;
                     };
@@ -903,9 +969,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     if (valid && !retrace && bi >= 0)
                         retrace = !own_gate(mcell, bi, ray, idd, resident ? S.bs[bi] : __ldg(gbs + bi));
                     if (retrace) {
-                        bi = retrace_f64(0, si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, ray, idd, eps, sc,
-                                         self_skip(S.emit, cur_emitter));
-                        nref += 2;
+                        bi = retrace_f64(0, si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, true, ray, idd, eps, sc,
+                                         self_skip(S.emit, cur_emitter), nref);
                     }
                 }
                 if (REC && valid) p.rec[gid0 * 4 + l - p.rec_base] = bi;

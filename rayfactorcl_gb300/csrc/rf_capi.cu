@@ -885,7 +885,7 @@ rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_
         p.bvtab = c->b_bvtab.as<HitRec>();
         p.bvinfo = c->b_bvinfo.as<int4>();
         p.nbv = c->nbv;
-        RF_CUDA(c, launch_batched_bv(p, rec, grid, c->stream));
+        RF_CUDA(c, launch_batched_bv(p, rec, c->cfg.work_counts != 0, grid, c->stream));
     } else {
         RF_CUDA(c, launch_batched(p, rec, batch_resident(c), c->cfg.work_counts != 0, grid, c->stream));
     }
@@ -1998,6 +1998,15 @@ rf_status rf_get_launch_config(rf_ctx *c, int32_t *block, int32_t *rays_per_thre
                                int32_t *smem_table, int32_t *one_ray_at_a_time)
 {
     if (!c) return RF_ERR_INVALID_ARG;
+    if (c->cfg.precision == RF_PREC_MIXED) {  // the mixed kernel the next trace takes
+        const bool small = use_small(c);
+        if (block) *block = small ? kSmallThreads : kBatchBlock;
+        if (rays_per_thread) *rays_per_thread = small ? 4 * small_gpt(c, false) : 4 * kBatchChunkDraws / kBatchBlock;
+        if (smem_hist) *smem_hist = 1;
+        if (smem_table) *smem_table = small || batch_resident(c) ? 1 : 0;
+        if (one_ray_at_a_time) *one_ray_at_a_time = 0;
+        return RF_OK;
+    }
     if (block) *block = c->block > 0 ? c->block : (c->cfg.block_size > 0 ? c->cfg.block_size : kBlock);
     if (rays_per_thread) *rays_per_thread = 4 * (c->gpt > 0 ? c->gpt : (c->cfg.rays_per_thread == 8 ? 2 : 1));
     if (smem_hist) *smem_hist = c->hist >= 0 ? c->hist : 1;

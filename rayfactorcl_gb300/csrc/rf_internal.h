@@ -119,7 +119,7 @@ template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
 // collect the work counters (TraceParams::work).
 cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool count, int grid, cudaStream_t st);
 // The same kernel with runBVGPU's bounding-surface semantics (one resident scene).
-cudaError_t launch_batched_bv(const TraceParams &p, bool rec, int grid, cudaStream_t st);
+cudaError_t launch_batched_bv(const TraceParams &p, bool rec, bool count, int grid, cudaStream_t st);
 int batched_blocks_per_sm(bool rec, bool resident);
 cudaError_t launch_build_masks(const MaskInputs &in, uint32_t *out, cudaStream_t st);
 // Mixed-precision kernel for one small scene with the plain kernel's launch shape
@@ -136,6 +136,7 @@ constexpr int kEmitFrameWords = 5;  // float4 words of a planar emitter's frame 
 constexpr int kBatchMaxBV = 16;     // bounding surfaces the mixed kernel takes (runBVGPU semantics)
 constexpr int kBatchMaxSurfaces = 32767;  // nearest hits are kept as int16 in shared memory
 constexpr int kBatchChunkDraws = 8192;  // Philox draws per chunk of the batched kernel
+constexpr int kBatchBlock = 1024;       // threads per block of the batched kernel
 
 // Emission frame of an emitter for the mixed kernels (rf_capi.cu): planar
 // emitters get their origin, in-plane axes and alignment rotation in FP64.

@@ -10,6 +10,7 @@ template cudaError_t launch_trace<MFast>(const LaunchCfg &, const TraceParams &,
 template int trace_blocks_per_sm<MFast>(const LaunchCfg &);
 
 static_assert(kBatchThreads * kBatchDraws == kBatchChunkDraws, "chunk size");
+static_assert(kBatchThreads == kBatchBlock, "block size");
 
 size_t batched_smem_bytes() { return sizeof(BatchSmem); }
 
@@ -33,10 +34,11 @@ cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool c
     return resident ? launch_b<false, true, false>(p, grid, st) : launch_b<false, false, false>(p, grid, st);
 }
 
-cudaError_t launch_batched_bv(const TraceParams &p, bool rec, int grid, cudaStream_t st)
+cudaError_t launch_batched_bv(const TraceParams &p, bool rec, bool count, int grid, cudaStream_t st)
 {
     if (p.nbv <= 0 || p.nbv > kBatchMaxBV || p.n > kBatchTile) return cudaErrorInvalidValue;
-    return rec ? launch_b<true, true, false, true>(p, grid, st) : launch_b<false, true, false, true>(p, grid, st);
+    if (rec) return launch_b<true, true, false, true>(p, grid, st);
+    return count ? launch_b<false, true, true, true>(p, grid, st) : launch_b<false, true, false, true>(p, grid, st);
 }
 
 template <bool REC, bool RES>

@@ -20,11 +20,10 @@ namespace rf {
 static_assert(kSmallThreads % 32 == 0, "whole warps");
 
 template <int GPT, bool REC>
-__global__ void __launch_bounds__(kSmallThreads) mixed_small_kernel(const TraceParams p)
+__global__ void __launch_bounds__(kSmallThreads, GPT == 1 ? 4 : 1) mixed_small_kernel(const TraceParams p)
 {
     constexpr int R = 4 * GPT;
     __shared__ HitRec s_tab[kSmallMax];
-    __shared__ float4 s_bs[kSmallMax];
     __shared__ int s_hist[kSmallMax];
     __shared__ rf_primitive s_emit;
     __shared__ float4 s_frame[kEmitFrameWords];
@@ -37,10 +36,7 @@ __global__ void __launch_bounds__(kSmallThreads) mixed_small_kernel(const TraceP
         const float4 *src = reinterpret_cast<const float4 *>(p.tab);
         float4 *dst = reinterpret_cast<float4 *>(s_tab);
         for (int i = tid; i < 4 * n; i += blockDim.x) dst[i] = __ldg(src + i);
-        for (int i = tid; i < n; i += blockDim.x) {
-            s_bs[i] = __ldg(p.bsph + i);
-            s_hist[i] = 0;
-        }
+        for (int i = tid; i < n; i += blockDim.x) s_hist[i] = 0;
     }
     const int64_t c0 = (p.total_chunks * (int64_t)blockIdx.x) / gridDim.x;
     const int64_t c1 = (p.total_chunks * (int64_t)(blockIdx.x + 1)) / gridDim.x;
@@ -99,9 +95,10 @@ __global__ void __launch_bounds__(kSmallThreads) mixed_small_kernel(const TraceP
             }
         }
         float tb[R];
-        int bi[R], dj[R];
+        int bi[R];
+        uint32_t dmask = 0u;  // bit k: ray k deferred a test
 #pragma unroll
-        for (int k = 0; k < R; ++k) { tb[k] = MFast::inf(); bi[k] = -1; dj[k] = -1; }
+        for (int k = 0; k < R; ++k) { tb[k] = MFast::inf(); bi[k] = -1; }
         const int skip = self_skip(s_emit, sg.emitter);  // block-uniform
         for (int j = 0; j < n; ++j) {
             if (j == skip) continue;
@@ -114,7 +111,7 @@ __global__ void __launch_bounds__(kSmallThreads) mixed_small_kernel(const TraceP
         bool defer = false;                                                    \
         const float t = hit_mixed(T, h, ray[k], eps, sc, defer);               \
         if (t < tb[k]) { tb[k] = t; bi[k] = j; }                               \
-        dj[k] = defer ? (dj[k] == -1 ? j : -2) : dj[k];                        \
+        dmask |= defer ? (1u << k) : 0u;                                       \
     }
             switch (type) {  // warp-uniform
             case RF_DISC: RF_MIXED_ALL(RF_DISC) break;
@@ -132,8 +129,8 @@ __global__ void __launch_bounds__(kSmallThreads) mixed_small_kernel(const TraceP
         for (int k = 0; k < R; ++k) {
             const int64_t rid = (gid0 + (int64_t)(k >> 2) * blockDim.x + tid) * 4 + (k & 3);
             const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
-            const int h = valid ? resolve_brute(bi[k], tb[k], dj[k], 0, n, true, s_tab, nullptr, s_bs, nullptr, ray[k],
-                                                eps, sc, skip, nref)
+            const int h = valid ? resolve_brute(bi[k], (dmask >> k) & 1u, 0, n, true, s_tab, nullptr, ray[k], eps, sc,
+                                                skip, nref)
                                 : -1;
             if (REC) {
                 if (valid) p.rec[rid - p.rec_base] = h;
