@@ -107,7 +107,10 @@ typedef struct rf_config {
                            * rf_last_work_counts (a few per cent slower); 0 = no counting      */
     int32_t batched_grid; /* RF_PREC_MIXED: 0 = one persistent block per SM; > 0 = at most this
                            * many blocks (results do not depend on it)                         */
-    uint32_t reserved[2];
+    int32_t split_stacks; /* RF_PREC_MIXED: 0 = a segment stack (consecutive cylinders that tile one
+                           * longer cylinder: a furnace wall of rings) is one cylinder test whose
+                           * root's z names the ring; 1 = every ring tested on its own          */
+    uint32_t reserved;
 } rf_config;
 
 typedef struct rf_ctx rf_ctx;
@@ -189,6 +192,15 @@ rf_status rf_ray_budgets(const rf_primitive *prims, int32_t n_prims, int32_t n_s
  * cylinders, frusta and spheres; exact for non-uniform scaling, unlike the
  * rayDensity proxies of Scene.cpp:361-387). */
 rf_status rf_surface_areas(const rf_primitive *prims, int32_t n_prims, double *areas_out);
+
+/* (No counterpart in the reference.)  The segment stacks RF_PREC_MIXED traces as
+ * one cylinder each (rf_config.split_stacks): runs of consecutive cylinders that
+ * tile one longer cylinder, never across a bounding surface's child range
+ * (bvs may be NULL when n_bvs = 0).  Host only.  first_out / count_out get up to
+ * cap stacks (first surface, number of surfaces); *n_stacks_out the number found. */
+rf_status rf_segment_stacks(const rf_primitive *prims, int32_t n_prims, const rf_bounding_volume *bvs,
+                            int32_t n_bvs, int32_t *first_out, int32_t *count_out, int32_t cap,
+                            int32_t *n_stacks_out);
 
 /* Budget planner: total_rays spread over the emitters in proportion to their
  * areas, in multiples of four (one Philox draw), at least four per non-empty

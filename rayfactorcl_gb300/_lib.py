@@ -35,7 +35,8 @@ EXPORTS = ("rf_config_default", "rf_create", "rf_destroy", "rf_last_error", "rf_
            "rf_write_output_txt", "rf_trace_batch", "rf_converge_batch", "rf_check_F",
            "rf_autotune", "rf_last_refine_count", "rf_last_work_counts", "rf_measure_fp32_peak",
            "rf_trace_mixed_noalloc", "rf_get_launch_config", "rf_trace_range", "rf_set_tallies",
-           "rf_surface_areas", "rf_budgets_by_area", "rf_budgets_by_density", "rf_smooth_F")
+           "rf_surface_areas", "rf_budgets_by_area", "rf_budgets_by_density", "rf_smooth_F",
+           "rf_segment_stacks")
 
 
 class RfConfig(ctypes.Structure):
@@ -45,7 +46,8 @@ class RfConfig(ctypes.Structure):
                 ("rays_per_thread", ctypes.c_int32), ("scene_id", ctypes.c_uint32),
                 ("tally_mode", ctypes.c_int32), ("table_mode", ctypes.c_int32),
                 ("test_order", ctypes.c_int32), ("work_counts", ctypes.c_int32),
-                ("batched_grid", ctypes.c_int32), ("reserved", ctypes.c_uint32 * 2)]
+                ("batched_grid", ctypes.c_int32), ("split_stacks", ctypes.c_int32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class RfSceneDesc(ctypes.Structure):
@@ -100,6 +102,7 @@ def load() -> ctypes.CDLL:
         "rf_smooth_F": (ctypes.c_int, [P, P, P, I32, I32, P, ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_double)]),
         "rf_budgets_by_area": (ctypes.c_int, [P, I32, I64, P]),
         "rf_budgets_by_density": (ctypes.c_int, [P, I32, P, I64, P]),
+        "rf_segment_stacks": (ctypes.c_int, [P, I32, P, I32, P, P, I32, ctypes.POINTER(I32)]),
         "rf_last_refine_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
         "rf_last_work_counts": (ctypes.c_int, [P, P]),
         "rf_measure_fp32_peak": (ctypes.c_int, [I32, ctypes.POINTER(ctypes.c_double)]),

@@ -28,11 +28,12 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "rf_kern_exact.cu": ["-fmad=false"],
     "rf_kern_fast.cu": [],
+    "rf_kern_batched.cu": [],
     "rf_kern_post.cu": [],
     "rf_capi.cu": [],
     "rf_noalloc.cu": [],
 }
-HEADERS = ["rf_internal.h", "rf_device.cuh", "rf_trace_kernels.cuh", "rf_batched.cuh"]
+HEADERS = ["rf_internal.h", "rf_device.cuh", "rf_trace_kernels.cuh", "rf_batched.cuh", "rf_mixed_small.cuh"]
 
 
 def nvcc() -> str:

@@ -311,15 +311,15 @@ __device__ __forceinline__ bool ill_conditioned(float d, float mag)
     return fabsf(d) < kCondRel * mag;
 }
 
-__device__ __noinline__ float cylinder_f64(const HitRec &h, const Ray<float> &w, float eps)
+static __device__ __noinline__ float cylinder_f64(const HitRec &h, const Ray<float> &w, float eps)
 {
     return (float)cylinder_hit<MF64>(h, to_f64(w), (double)eps);
 }
-__device__ __noinline__ float frustum_f64(const HitRec &h, const Ray<float> &w, float eps)
+static __device__ __noinline__ float frustum_f64(const HitRec &h, const Ray<float> &w, float eps)
 {
     return (float)frustum_hit<MF64>(h, to_f64(w), (double)eps);
 }
-__device__ __noinline__ float sphere_f64(const HitRec &h, const Ray<float> &w, float eps, bool sc)
+static __device__ __noinline__ float sphere_f64(const HitRec &h, const Ray<float> &w, float eps, bool sc)
 {
     return (float)sphere_hit<MF64>(h, to_f64(w), (double)eps, sc);
 }
@@ -406,7 +406,7 @@ __device__ __forceinline__ float hit_mixed(int type, const HitRec &h, const Ray<
 }
 
 // FP64 evaluation of a deferred test (cold path).
-__device__ __noinline__ float hit_f64(const HitRec &h, const Ray<float> &w, float eps, bool sc)
+static __device__ __noinline__ float hit_f64(const HitRec &h, const Ray<float> &w, float eps, bool sc)
 {
     switch (__float_as_int(h.aux.x)) {
     case RF_CYLINDER: return cylinder_f64(h, w, eps);
@@ -414,6 +414,92 @@ __device__ __noinline__ float hit_f64(const HitRec &h, const Ray<float> &w, floa
     case RF_SPHERE: return sphere_f64(h, w, eps, sc);
     default: return MFast::inf();
     }
+}
+
+// Segment stacks.  Consecutive cylinders [a, a + m) whose frames are one
+// cylinder's shifted by whole lengths along its axis are the same quadric, so the
+// index-order nearest hit among them is one cylinder test with z in [0, m] of the
+// first member's frame: the near root if it lies on the stack (a root on the
+// boundary of two members goes to the lower one, as the tie rule of the member
+// loop does), else the far root strictly inside a member (quadric_pick rejects a
+// far root on a member's rim).  ring = the member hit, 0-based.
+template <class M>
+__device__ __forceinline__ typename M::T stack_pick(const Ray<typename M::T> &o, typename M::T t1, typename M::T t2,
+                                                    typename M::T eps, int m, int &ring)
+{
+    using T = typename M::T;
+    const T fm = T(m);
+    const T z1 = o.sz + o.cz * t1;
+    const T z2 = o.sz + o.cz * t2;
+    const bool v1 = !(t1 < eps || z1 < T(0) || z1 > fm);
+    const T f2 = floor(z2);
+    const bool v2 = t2 > eps && z2 > T(0) && z2 < fm && z2 != f2;
+    const int r1 = z1 > T(0) ? (int)ceil(z1) - 1 : 0;
+    ring = min(m - 1, max(0, v1 ? r1 : (int)f2));
+    return v1 ? t1 : (v2 ? t2 : M::inf());
+}
+
+__device__ __forceinline__ float stack_mixed(const HitRec &h, const Ray<float> &w, float eps, bool &defer, int &ring)
+{
+    const Ray<float> o = xfrm_ray<MFast>(h, w);  // as cylinder_mixed
+    const float A = fmaf(o.cx, o.cx, o.cy * o.cy);
+    const float B = -fmaf(o.sx, o.cx, o.sy * o.cy);
+    const float pw = o.sy * o.cx;
+    const float wz = fmaf(o.sx, o.cy, -pw);
+    const float d = fmaf(-wz, wz, A);
+    const bool ill = ill_conditioned(d, fmaf(2.0f * fabsf(wz), fabsf(wz) + fabsf(pw), A));
+    const float disc = MFast::sqrt(d);
+    const float ra = MFast::rcp(A);
+    const float t = stack_pick<MFast>(o, ra * (B - disc), ra * (B + disc), eps, (int)h.aux.y, ring);
+    defer = ill;
+    return ill ? MFast::inf() : t;
+}
+
+static __device__ __noinline__ float stack_f64(const HitRec &h, const Ray<float> &w, float eps, int &ring)
+{
+    using T = double;  // as cylinder_hit<MF64>
+    const Ray<T> o = xfrm_ray<MF64>(h, to_f64(w));
+    const T A = MF64::fma(o.cx, o.cx, o.cy * o.cy);
+    const T B = -MF64::fma(o.sx, o.cx, o.sy * o.cy);
+    const T C = MF64::fma(o.sx, o.sx, MF64::fma(o.sy, o.sy, T(-1)));
+    const T disc = MF64::sqrt(B * B - A * C);
+    const T ra = MF64::rcp(A);
+    return (float)stack_pick<MF64>(o, ra * (B - disc), ra * (B + disc), (T)eps, (int)h.aux.y, ring);
+}
+
+// First member of the stack that surface j (a member, record h) belongs to, and
+// one past its last.
+__device__ __forceinline__ int stack_first(const HitRec &h, int j) { return j - __float_as_int(h.aux.w); }
+__device__ __forceinline__ int stack_end(const HitRec &h, int j) { return stack_first(h, j) + (int)h.aux.y; }
+
+// The mixed test of surface j (record h) -- for a stack member, the stack's --
+// with idx the surface hit (j, or the member of the stack).
+template <bool STK>
+__device__ __forceinline__ float test_mixed(int type, const HitRec &h, int j, const Ray<float> &w, float eps, bool sc,
+                                            bool &defer, int &idx)
+{
+    if (STK && type == kStackType) {
+        int ring;
+        const float t = stack_mixed(h, w, eps, defer, ring);
+        idx = stack_first(h, j) + ring;
+        return t;
+    }
+    idx = j;
+    return hit_mixed(type, h, w, eps, sc, defer);
+}
+
+// FP64 evaluation of a deferred test of surface j, idx as in test_mixed.
+template <bool STK>
+__device__ __forceinline__ float test_f64(const HitRec &h, int j, const Ray<float> &w, float eps, bool sc, int &idx)
+{
+    if (STK && __float_as_int(h.aux.x) == kStackType) {
+        int ring;
+        const float t = stack_f64(h, w, eps, ring);
+        idx = stack_first(h, j) + ring;
+        return t;
+    }
+    idx = j;
+    return hit_f64(h, w, eps, sc);
 }
 
 // Sort key of a ray: its direction cell above the 4 x 4 cell of the two surface
@@ -443,12 +529,47 @@ __device__ __forceinline__ bool own_gate(const uint32_t *mcell, int j, const Ray
     return ray_may_hit(ray, idd, b);
 }
 
+// Bits of a 32-surface candidate word from position k on (k <= 0: all, k >= 32: none).
+__device__ __forceinline__ unsigned keep_from(int k)
+{
+    return k <= 0 ? ~0u : (k >= 32 ? 0u : (~0u << k));
+}
+
+// The candidate loop's test: hit_mixed's, plus segment stacks.  idx (j on entry)
+// gets the surface hit; a stack's other members leave the candidate word cm and
+// the pair's second candidate (vb = 0 when jb is one): skip_to = one past the
+// stack, for later words.
+__device__ __forceinline__ float hit_hot(int type, const HitRec &h, int j, const Ray<float> &w, float eps, bool sc,
+                                         bool &defer, int &idx, int jw, unsigned &cm, int &skip_to, int jb,
+                                         unsigned &vb)
+{
+    switch (type) {
+    case RF_RECTANGLE: return rectangle_hit<MFast>(h, w, eps);
+    case RF_DISC: return disc_hit<MFast>(h, w, eps);
+    case RF_ANNULUS: return annulus_hit<MFast>(h, w, eps);
+    case RF_CYLINDER: return cylinder_mixed(h, w, eps, defer);
+    case RF_FRUSTUM: return frustum_mixed(h, w, eps, defer);
+    case RF_SPHERE: return sphere_mixed(h, w, eps, sc, defer);
+    case kStackType: {
+        int ring;
+        const float t = stack_mixed(h, w, eps, defer, ring);
+        idx = stack_first(h, j) + ring;
+        skip_to = stack_end(h, j);
+        cm &= keep_from(skip_to - jw);
+        if (jb < skip_to) vb = 0u;
+        return t;
+    }
+    default: return MFast::inf();
+    }
+}
+
 // Full nearest-hit search for one ray over the surfaces [lo, hi) its gate admits
 // (gated: the cell mask when mcell is set, and the bounding-sphere check; else
 // every surface but skip), with FP64 for every ill-conditioned quadric; nf64
 // counts the FP64 evaluations.  Cold path: rays that deferred a test they could
 // not resolve in their hot loop.
-__device__ __noinline__ int retrace_f64(int lo, int hi, bool resident, const HitRec *stab, const HitRec *gtab,
+template <bool STK>
+static __device__ __noinline__ int retrace_f64(int lo, int hi, bool resident, const HitRec *stab, const HitRec *gtab,
                                         const float4 *sbs, const float4 *gbs, const uint32_t *mcell, bool gated,
                                         const Ray<float> &ray, float idd, float eps, bool sc, int skip, int &nf64)
 {
@@ -458,13 +579,16 @@ __device__ __noinline__ int retrace_f64(int lo, int hi, bool resident, const Hit
         if (j == skip) continue;
         if (gated && !own_gate(mcell, j, ray, idd, resident ? sbs[j] : __ldg(gbs + j))) continue;
         const HitRec h = resident ? stab[j] : load_rec(gtab, j);
+        const int type = __float_as_int(h.aux.x);
         bool defer = false;
-        float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
+        int idx;
+        float t = test_mixed<STK>(type, h, j, ray, eps, sc, defer, idx);
         if (defer) {
-            t = hit_f64(h, ray, eps, sc);
+            t = test_f64<STK>(h, j, ray, eps, sc, idx);
             ++nf64;
         }
-        if (t < tb) { tb = t; bi = j; }
+        if (t < tb) { tb = t; bi = idx; }
+        if (STK && type == kStackType) j = stack_end(h, j) - 1;  // one test for the whole stack
     }
     return bi;
 }
@@ -474,12 +598,13 @@ __device__ __noinline__ int retrace_f64(int lo, int hi, bool resident, const Hit
 // a ray is traced again with FP64 for each deferred test.  Shared by the
 // small-scene paths of the batched kernel and of mixed_small_kernel, so both
 // give the same result.
+template <bool STK>
 __device__ __forceinline__ int resolve_brute(int bi, bool deferred, int lo, int hi, bool resident,
                                              const HitRec *stab, const HitRec *gtab, const Ray<float> &ray,
                                              float eps, bool sc, int skip, int &nref)
 {
     if (deferred)
-        bi = retrace_f64(lo, hi, resident, stab, gtab, nullptr, nullptr, nullptr, false, ray, 0.0f, eps, sc, skip,
+        bi = retrace_f64<STK>(lo, hi, resident, stab, gtab, nullptr, nullptr, nullptr, false, ray, 0.0f, eps, sc, skip,
                          nref);
     return bi;
 }
@@ -525,8 +650,9 @@ __device__ __forceinline__ int bv_select(const HitRec *bvtab, const int4 *bvinfo
 // the tests by surface type, the candidates and the packets (p.work); the
 // counters cost a few per cent, so timed runs leave them out.  BV: one resident
 // scene with bounding surfaces (p.bvtab, p.bvinfo, p.nbv <= kBatchMaxBV) traced
-// with runBVGPU's semantics (bv_select).
-template <bool REC, bool RESIDENT, bool COUNT, bool BV>
+// with runBVGPU's semantics (bv_select).  STK: some scene has segment stacks
+// (kStackType records); the candidate loops then test a stack once.
+template <bool REC, bool RESIDENT, bool COUNT, bool BV, bool STK>
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TraceParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -674,12 +800,15 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             for (int j = lo; j < hi; ++j) {
                                 if (j == skip) continue;
                                 const HitRec h = S.tab[j];
+                                const int type = __float_as_int(h.aux.x);
                                 bool defer = false;
-                                const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
-                                if (t < tr) { tr = t; br = j; }
+                                int idx;
+                                const float t = test_mixed<STK>(type, h, j, ray, eps, sc, defer, idx);
+                                if (t < tr) { tr = t; br = idx; }
                                 dr |= defer;
+                                if (STK && type == kStackType) j = stack_end(h, j) - 1;
                             }
-                            return resolve_brute(br, dr, lo, hi, true, S.tab, gtab, ray, eps, sc, skip, nref);
+                            return resolve_brute<STK>(br, dr, lo, hi, true, S.tab, gtab, ray, eps, sc, skip, nref);
                         };
                         bi = bv_select(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0, find);
                     } else if (valid) {
@@ -693,12 +822,15 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         for (int j = 0; j < si.n; ++j) {
                             if (j == skip) continue;  // uniform: every thread's emitter
                             const HitRec h = RESIDENT ? S.tab[j] : load_rec(gtab, j);
+                            const int type = __float_as_int(h.aux.x);
                             bool defer = false;
-                            const float t = hit_mixed(__float_as_int(h.aux.x), h, ray, eps, sc, defer);
-                            if (t < tb) { tb = t; bi = j; }
+                            int idx;
+                            const float t = test_mixed<STK>(type, h, j, ray, eps, sc, defer, idx);
+                            if (t < tb) { tb = t; bi = idx; }
                             dany |= defer;
+                            if (STK && type == kStackType) j = stack_end(h, j) - 1;
                         }
-                        bi = resolve_brute(bi, dany, 0, si.n, RESIDENT, S.tab, gtab, ray, eps, sc, skip, nref);
+                        bi = resolve_brute<STK>(bi, dany, 0, si.n, RESIDENT, S.tab, gtab, ray, eps, sc, skip, nref);
                     }
                     // all 32 lanes reach the warp-wide calls below
                     if (COUNT) nv_warp += __popc(__ballot_sync(0xffffffffu, valid));
@@ -715,8 +847,14 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 if (lane == 0 && nv_warp)
                     for (int j = 0; j < si.n; ++j) {
                         if (j == skip) continue;
-                        const int type = RESIDENT ? __float_as_int(S.tab[j].aux.x) : __float_as_int(__ldg(&gtab[j].aux.x));
-                        if ((unsigned)type < 6u) S.wcount[warp][type] += nv_warp;
+                        const HitRec h = RESIDENT ? S.tab[j] : load_rec(gtab, j);
+                        const int type = __float_as_int(h.aux.x);
+                        if (STK && type == kStackType) {
+                            S.wcount[warp][RF_CYLINDER] += nv_warp;
+                            j = stack_end(h, j) - 1;
+                        } else if ((unsigned)type < 6u) {
+                            S.wcount[warp][type] += nv_warp;
+                        }
                     }
                 fold_counts();
             }
@@ -851,13 +989,13 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     }
                     auto find = [&](int lo, int hi) {  // warp-wide: every lane, same lo and hi
                         float tr = MFast::inf();
-                        int br = -1, dr = -1, nd = 0;
+                        int br = -1, dr = -1, nd = 0, skip_to = lo;
 #pragma unroll 1
                         for (int w = lo >> 5; lo < hi && w <= (hi - 1) >> 5; ++w) {
                             const int jw = w << 5;
                             unsigned cm = mcell ? __reduce_or_sync(0xffffffffu, __ldg(mcell + w))
                                                 : __shfl_sync(0xffffffffu, cmask, w);
-                            if (lo > jw) cm &= ~0u << (lo - jw);
+                            cm &= keep_from((STK ? skip_to : lo) - jw);  // lo, and stacks tested in an earlier word
                             if (hi < jw + 32) cm &= (1u << (hi - jw)) - 1u;
                             if (skip >= jw && skip < jw + 32) cm &= ~(1u << (skip - jw));
                             if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
@@ -867,10 +1005,13 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                                 if (!__any_sync(0xffffffffu, ray_may_hit(ray, idd, S.bs[j]))) continue;
                                 const HitRec h = S.tab[j];
                                 const int type = __float_as_int(h.aux.x);
-                                if (COUNT) tcount += lane == type ? nvalid : 0;
+                                if (COUNT) tcount += lane == (type == kStackType ? RF_CYLINDER : type) ? nvalid : 0;
                                 bool defer = false;
-                                const float t = hit_mixed(type, h, ray, eps, sc, defer);
-                                if (t < tr) { tr = t; br = j; }
+                                int idx = j;
+                                unsigned nb = 0u;
+                                const float t = STK ? hit_hot(type, h, j, ray, eps, sc, defer, idx, jw, cm, skip_to, hi, nb)
+                                                    : hit_mixed(type, h, ray, eps, sc, defer);
+                                if (t < tr) { tr = t; br = idx; }
                                 nd += defer;
                                 dr = defer ? j : dr;
                             }
@@ -878,14 +1019,15 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         // as below: nearest among the children the lane's own gate admits
                         bool again = valid && nd > 1;
                         if (valid && nd == 1) {
-                            const float t = hit_f64(S.tab[dr], ray, eps, sc);
-                            if (t < tr || (t == tr && br >= 0 && dr < br)) { tr = t; br = dr; }
+                            int dq;
+                            const float t = test_f64<STK>(S.tab[dr], dr, ray, eps, sc, dq);
+                            if (t < tr || (t == tr && br >= 0 && dq < br)) { tr = t; br = dq; }
                             ++nref;
                             again = !own_gate(mcell, dr, ray, idd, S.bs[dr]);
                         }
                         if (valid && !again && br >= 0) again = !own_gate(mcell, br, ray, idd, S.bs[br]);
                         if (again) {
-                            br = retrace_f64(lo, hi, true, S.tab, gtab, S.bs, gbs, mcell, true, ray, idd, eps, sc, skip,
+                            br = retrace_f64<STK>(lo, hi, true, S.tab, gtab, S.bs, gbs, mcell, true, ray, idd, eps, sc, skip,
                                              nref);
                         }
                         return br;
@@ -896,6 +1038,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     int dj = -1, ndef = 0;  // deferred FP64 tests of this lane: the last one, and how many
                     if (COUNT && lane == 0) S.wcount[warp][7] += 1;
                     // surfaces in blocks of 1024 (one block when the scene has masks)
+                    int skip_to = 0;  // members of a stack already tested are not candidates
 #pragma unroll 1
                     for (int j0 = 0; j0 < si.n; j0 += 1024) {
                         const int nwords = min(32, (si.n - j0 + 31) >> 5);
@@ -918,7 +1061,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             const int jw = j0 + (w << 5);
                             const unsigned cm0 = mcell ? __reduce_or_sync(0xffffffffu, __ldg(mcell + (jw >> 5)))
                                                        : __shfl_sync(0xffffffffu, cmask, w);  // block-uniform choice
-                            unsigned cm = cm0;
+                            unsigned cm = STK ? cm0 & keep_from(skip_to - jw) : cm0;
                             if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
                             // two candidates per pass: their sphere checks are independent
                             // chains (latency hidden); tests still run in index order
@@ -933,17 +1076,20 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                                 const bool ma = ray_may_hit(ray, idd, sa);
                                 const bool mb = bb_ >= 0 && ray_may_hit(ray, idd, sb);
                                 const unsigned va = __ballot_sync(0xffffffffu, ma);
-                                const unsigned vb = __ballot_sync(0xffffffffu, mb);
+                                unsigned vb = __ballot_sync(0xffffffffu, mb);
 #pragma unroll
                                 for (int q = 0; q < 2; ++q) {
                                     if (!(q ? vb : va)) continue;  // warp-uniform
                                     const int j = q ? jb : ja;
                                     const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
                                     const int type = __float_as_int(h.aux.x);
-                                    if (COUNT) tcount += lane == type ? nvalid : 0;
+                                    if (COUNT) tcount += lane == (type == kStackType ? RF_CYLINDER : type) ? nvalid : 0;
                                     bool defer = false;
-                                    const float t = hit_mixed(type, h, ray, eps, sc, defer);
-                                    if (t < tb) { tb = t; bi = j; }
+                                    int idx = j;
+                                    const float t = STK ? hit_hot(type, h, j, ray, eps, sc, defer, idx, jw, cm, skip_to,
+                                                                  q ? INT_MAX : jb, vb)
+                                                        : hit_mixed(type, h, ray, eps, sc, defer);
+                                    if (t < tb) { tb = t; bi = idx; }
                                     ndef += defer;  // predicated, no branch
                                     dj = defer ? j : dj;
                                 }
@@ -961,15 +1107,16 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                     bool retrace = valid && ndef > 1;
                     if (valid && ndef == 1) {
                         const HitRec hq = RESIDENT ? S.tab[dj] : load_rec(gtab, dj);
-                        const float t = hit_f64(hq, ray, eps, sc);
-                        if (t < tb || (t == tb && bi >= 0 && dj < bi)) { tb = t; bi = dj; }
+                        int dq;
+                        const float t = test_f64<STK>(hq, dj, ray, eps, sc, dq);
+                        if (t < tb || (t == tb && bi >= 0 && dq < bi)) { tb = t; bi = dq; }
                         ++nref;
                         retrace = !own_gate(mcell, dj, ray, idd, resident ? S.bs[dj] : __ldg(gbs + dj));
                     }
                     if (valid && !retrace && bi >= 0)
                         retrace = !own_gate(mcell, bi, ray, idd, resident ? S.bs[bi] : __ldg(gbs + bi));
                     if (retrace) {
-                        bi = retrace_f64(0, si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, true, ray, idd, eps, sc,
+                        bi = retrace_f64<STK>(0, si.n, RESIDENT, S.tab, gtab, S.bs, gbs, mcell, true, ray, idd, eps, sc,
                                          self_skip(S.emit, cur_emitter), nref);
                     }
                 }
@@ -1027,7 +1174,7 @@ __device__ __forceinline__ bool plane_separates(float4 ball, float4 axis_cos, fl
     return false;
 }
 
-__global__ void __launch_bounds__(256) build_masks_kernel(MaskInputs in, uint32_t *out)
+static __global__ void __launch_bounds__(256) build_masks_kernel(MaskInputs in, uint32_t *out)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= in.total_words) return;

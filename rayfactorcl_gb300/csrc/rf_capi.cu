@@ -130,6 +130,9 @@ struct rf_ctx {
     // single-scene MIXED traces: 0 = by surface count, 1 = small-scene kernel,
     // 2 = batched kernel (set by rf_autotune)
     int mixed_path = 0;
+    int b_stacks = 0;  // segment stacks in the mixed tables
+    std::vector<int> b_test_type;  // scene 0 of the mixed tables: type each surface's test counts as
+                                   // (a stack: RF_CYLINDER at its first member, -1 at the others)
     bool last_small = false;                 // the last MIXED launch was the small-scene kernel
     unsigned long long small_work[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
@@ -341,6 +344,30 @@ float4 widen_sq(float4 b)
     return make_float4(b.x, b.y, b.z, (float)(r * r));
 }
 
+// Bounding sphere (centre, radius) of the object-space box [-ext, ext]^2 x [z0, z1]
+// under a re-centred record's m, with a margin for FP32 rounding.
+float4 object_box_sphere(const rf_primitive &e, double ext, double z0, double z1)
+{
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, pts[8][3];
+    for (int q = 0; q < 8; ++q) {
+        const double o[3] = {(q & 1) ? ext : -ext, (q & 2) ? ext : -ext, (q & 4) ? z1 : z0};
+        for (int k = 0; k < 3; ++k) {
+            const float *r = e.m + 4 * k;
+            pts[q][k] = r[0] * o[0] + r[1] * o[1] + r[2] * o[2] + r[3];
+            lo[k] = std::min(lo[k], pts[q][k]);
+            hi[k] = std::max(hi[k], pts[q][k]);
+        }
+    }
+    const double cx = 0.5 * (lo[0] + hi[0]), cy = 0.5 * (lo[1] + hi[1]), cz = 0.5 * (lo[2] + hi[2]);
+    double rad = 0.0;
+    for (int q = 0; q < 8; ++q) {
+        const double dx = pts[q][0] - cx, dy = pts[q][1] - cy, dz = pts[q][2] - cz;
+        rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    const double cn = std::sqrt(cx * cx + cy * cy + cz * cz);
+    return make_float4((float)cx, (float)cy, (float)cz, (float)(rad * (1.0 + 1e-5) + 1e-6 * (cn + rad) + 1e-7));
+}
+
 // Mixed-precision tables of one scene.  The world origin moves (in FP64) to the
 // mean of the surfaces' translations, so a scene placed far from the origin keeps
 // its FP32 resolution: m' = m - anchor, invm' = invm o (x + anchor).  Each surface
@@ -368,25 +395,62 @@ void prepare_mixed(const rf_primitive *prims, int n, rf_primitive *emit, HitRec 
         case RF_ANNULUS: ext = std::sqrt(std::max(0.0, (double)e.util2)); break;
         default: break;
         }
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, pts[8][3];
-        for (int q = 0; q < 8; ++q) {
-            const double o[3] = {(q & 1) ? ext : -ext, (q & 2) ? ext : -ext, (q & 4) ? z1 : z0};
-            for (int k = 0; k < 3; ++k) {
-                const float *r = e.m + 4 * k;
-                pts[q][k] = r[0] * o[0] + r[1] * o[1] + r[2] * o[2] + r[3];
-                lo[k] = std::min(lo[k], pts[q][k]);
-                hi[k] = std::max(hi[k], pts[q][k]);
+        bs[i] = object_box_sphere(e, ext, z0, z1);
+    }
+}
+
+// Segment stacks of one scene's mixed tables (kStackType): runs of consecutive
+// cylinders [a, a + m), 2 <= m <= 65535, with the same linear part of m (axes
+// and radii), the same normal sign (util2) and each translation one axis column
+// (m's third column) past the previous one's, so that member k is the first
+// member shifted by k lengths along its axis (to 1e-6 of the transform's scale).
+// A stack never continues across an index i with cut[i] set (a bounding
+// surface's children start or end there).  Each member's record becomes the
+// stack's -- the first member's invm, aux = (kStackType, m, util2, k) -- and its
+// bounding sphere the stack's.  Returns the number of stacks.
+int mark_stacks(const rf_primitive *e, int n, HitRec *tab, float4 *bs, const std::vector<char> &cut)
+{
+    int nstacks = 0;
+    for (int i = 0; i < n;) {
+        int j = i + 1;
+        if (e[i].type == RF_CYLINDER) {
+            double scale = 0.0;  // largest column of the linear part
+            for (int col = 0; col < 3; ++col) {
+                double c2 = 0.0;
+                for (int r = 0; r < 3; ++r) c2 += (double)e[i].m[4 * r + col] * e[i].m[4 * r + col];
+                scale = std::max(scale, std::sqrt(c2));
+            }
+            while (j < n && j - i < 65535 && !((size_t)j < cut.size() && cut[j]) && e[j].type == RF_CYLINDER &&
+                   e[j].util2 == e[i].util2) {
+                bool ok = true;
+                for (int r = 0; r < 3 && ok; ++r) {
+                    for (int col = 0; col < 3 && ok; ++col)
+                        ok = std::fabs((double)e[j].m[4 * r + col] - e[i].m[4 * r + col]) <= 1e-6 * scale;
+                    const double want = (double)e[j - 1].m[4 * r + 3] + e[i].m[4 * r + 2];
+                    ok = ok && std::fabs((double)e[j].m[4 * r + 3] - want) <= 1e-6 * (scale + std::fabs(want));
+                }
+                if (!ok) break;
+                ++j;
             }
         }
-        const double cx = 0.5 * (lo[0] + hi[0]), cy = 0.5 * (lo[1] + hi[1]), cz = 0.5 * (lo[2] + hi[2]);
-        double rad = 0.0;
-        for (int q = 0; q < 8; ++q) {
-            const double dx = pts[q][0] - cx, dy = pts[q][1] - cy, dz = pts[q][2] - cz;
-            rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
+        const int m = j - i;
+        if (m >= 2) {
+            HitRec u = tab[i];
+            int32_t ti = kStackType;
+            std::memcpy(&u.aux.x, &ti, 4);
+            u.aux.y = (float)m;
+            const float4 sph = object_box_sphere(e[i], 1.0, 0.0, (double)m);
+            for (int k = 0; k < m; ++k) {
+                tab[i + k] = u;
+                const int32_t off = k;
+                std::memcpy(&tab[i + k].aux.w, &off, 4);
+                bs[i + k] = sph;
+            }
+            ++nstacks;
         }
-        const double cn = std::sqrt(cx * cx + cy * cy + cz * cz);
-        bs[i] = make_float4((float)cx, (float)cy, (float)cz, (float)(rad * (1.0 + 1e-5) + 1e-6 * (cn + rad) + 1e-7));
+        i = j;
     }
+    return nstacks;
 }
 
 // Self-hit threshold of a scene: eps >= 0 is absolute (the reference's 1e-3,
@@ -676,18 +740,21 @@ void rf::emit_frame(const rf_primitive &e, float4 *f)
 // Mixed-precision tables of one scene as the batched kernel reads them
 // (re-centred transforms, hit records, bounding spheres with squared radius)
 // and the scene's self-hit threshold (eps < 0: relative, as rf_trace forms it).
-void rf::prepare_mixed_tables(const rf_primitive *prims, int n, float eps, rf_primitive *emit, HitRec *tab,
-                              float4 *bs, float *eps_out)
+int rf::prepare_mixed_tables(const rf_primitive *prims, int n, float eps, rf_primitive *emit, HitRec *tab,
+                             float4 *bs, float *eps_out)
 {
     prepare_mixed(prims, n, emit, tab, bs);
     *eps_out = scene_eps(eps, bs, n);
+    const int nstacks = mark_stacks(emit, n, tab, bs, std::vector<char>());
     for (int i = 0; i < n; ++i) bs[i] = widen_sq(bs[i]);
+    return nstacks;
 }
 
 namespace {
 
 // Upload the scenes of a batch (one scene for rf_set_scene in MIXED mode).
-rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with_budgets)
+rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with_budgets,
+                       const std::vector<char> &cut0 = std::vector<char>())
 {
     if (ns <= 0 || !scenes) return fail(c, RF_ERR_INVALID_ARG, "no scenes");
     int64_t nprim = 0, nhits = 0;
@@ -708,6 +775,7 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
     std::vector<float4> bs(nprim), patch((size_t)nprim * 16), chain((size_t)nprim * kChainMax), plane(nprim),
         frame((size_t)nprim * kEmitFrameWords);
     c->b_info.resize(ns);
+    c->b_stacks = 0;
     int64_t off = 0, hoff = 0;
     for (int s = 0; s < ns; ++s) {
         const int n = scenes[s].n_prims;
@@ -717,11 +785,23 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
         for (int i = 0; i < n; ++i) {
             const int64_t g = off + i;
             patch_balls(emit[g], patch.data() + g * 16);
-            surface_chain(emit[g], bs[g], chain.data() + g * kChainMax);
+            surface_chain(emit[g], bs[g], chain.data() + g * kChainMax);  // the masks: per surface
             plane[g] = surface_plane(emit[g]);
             emit_frame(emit[g], frame.data() + g * kEmitFrameWords);
-            bs[g] = widen_sq(bs[g]);
         }
+        if (!c->cfg.split_stacks)
+            c->b_stacks += mark_stacks(emit.data() + off, n, tab.data() + off, bs.data() + off,
+                                       s == 0 ? cut0 : std::vector<char>());
+        if (s == 0) {
+            c->b_test_type.assign(n, 0);
+            for (int i = 0; i < n; ++i) {
+                int32_t ti, k;
+                std::memcpy(&ti, &tab[i].aux.x, 4);
+                std::memcpy(&k, &tab[i].aux.w, 4);
+                c->b_test_type[i] = ti != kStackType ? ti : (k == 0 ? (int)RF_CYLINDER : -1);
+            }
+        }
+        for (int i = 0; i < n; ++i) bs[off + i] = widen_sq(bs[off + i]);
         c->b_info[s].n = n;
         c->b_info[s].prim_off = (int32_t)off;
         c->b_info[s].hits_off = hoff;
@@ -885,9 +965,10 @@ rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_
         p.bvtab = c->b_bvtab.as<HitRec>();
         p.bvinfo = c->b_bvinfo.as<int4>();
         p.nbv = c->nbv;
-        RF_CUDA(c, launch_batched_bv(p, rec, c->cfg.work_counts != 0, grid, c->stream));
+        RF_CUDA(c, launch_batched_bv(p, rec, c->cfg.work_counts != 0, c->b_stacks > 0, grid, c->stream));
     } else {
-        RF_CUDA(c, launch_batched(p, rec, batch_resident(c), c->cfg.work_counts != 0, grid, c->stream));
+        RF_CUDA(c, launch_batched(p, rec, batch_resident(c), c->cfg.work_counts != 0, c->b_stacks > 0, grid,
+                                  c->stream));
     }
     RF_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     c->last_launches = 1;
@@ -930,10 +1011,16 @@ rf_status run_small(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_ch
     if (zero_hits) RF_CUDA(c, cudaMemsetAsync(c->b_hits.p, 0, (size_t)c->b_hits_total * 8, c->stream));
     RF_CUDA(c, cudaMemsetAsync(c->b_counters.p, 0, sizeof(BatchCounters), c->stream));
     if (seg.empty() || total_chunks == 0) return RF_OK;
-    if (c->cfg.work_counts) {  // every ray is tested against every surface
-        int64_t rays = 0;
-        for (const Segment &sg : seg) rays += sg.ray_end - sg.ray_begin;
-        for (const rf_primitive &pr : c->prims) c->small_work[pr.type] += (unsigned long long)rays;
+    if (c->cfg.work_counts) {  // every ray against every surface but a planar emitter itself, a stack once
+        for (const Segment &sg : seg) {
+            const int64_t rays = sg.ray_end - sg.ray_begin;
+            const int et = c->prims[sg.emitter].type;
+            const bool planar = et == RF_DISC || et == RF_ANNULUS || et == RF_RECTANGLE;
+            for (int j = 0; j < (int)c->b_test_type.size(); ++j) {
+                if ((planar && j == sg.emitter) || c->b_test_type[j] < 0) continue;
+                c->small_work[c->b_test_type[j]] += (unsigned long long)rays;
+            }
+        }
     }
     RF_CUDA(c, c->h_seg.ensure(seg.size() * sizeof(Segment)));
     RF_CUDA(c, c->d_seg.ensure(seg.size() * sizeof(Segment)));
@@ -1043,7 +1130,8 @@ rf_status rf_create(rf_ctx **out, const rf_config *cfg)
         return RF_ERR_INVALID_ARG;
     if (c.block_size < 0 || c.block_size > kBlock || (c.block_size % 32) != 0) return RF_ERR_INVALID_ARG;
     if (c.tally_mode < 0 || c.tally_mode > 2 || c.table_mode < 0 || c.table_mode > 2) return RF_ERR_INVALID_ARG;
-    if (c.work_counts < 0 || c.work_counts > 1 || c.batched_grid < 0) return RF_ERR_INVALID_ARG;
+    if (c.work_counts < 0 || c.work_counts > 1 || c.batched_grid < 0 || c.split_stacks < 0 || c.split_stacks > 1)
+        return RF_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
         cudaGetLastError();
@@ -1152,7 +1240,12 @@ rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf
     }
     if (c->cfg.precision == RF_PREC_MIXED) {
         rf_scene_desc d{prims, n, 0, nullptr};
-        if ((st = upload_batch(c, &d, 1, false)) != RF_OK) return st;
+        std::vector<char> cut(n + 1, 0);  // segment stacks stay inside bounding-surface child ranges
+        for (int b = 0; b < nbv; ++b) {
+            if (bvs[b].objStartIndex >= 0 && bvs[b].objStartIndex <= n) cut[bvs[b].objStartIndex] = 1;
+            if (bvs[b].objEndIndex >= 0 && bvs[b].objEndIndex <= n) cut[bvs[b].objEndIndex] = 1;
+        }
+        if ((st = upload_batch(c, &d, 1, false, cut)) != RF_OK) return st;
         c->b_single = true;
         if (nbv > 0) {  // bounding surfaces in the surfaces' re-centred frame (prepare_mixed's anchor)
             double a[3] = {0, 0, 0};
@@ -1481,6 +1574,39 @@ rf_status rf_surface_areas(const rf_primitive *prims, int32_t n, double *areas)
     return RF_OK;
 }
 
+rf_status rf_segment_stacks(const rf_primitive *prims, int32_t n, const rf_bounding_volume *bvs, int32_t nbv,
+                            int32_t *first_out, int32_t *count_out, int32_t cap, int32_t *n_stacks_out)
+{
+    if (!prims || n <= 0 || nbv < 0 || (nbv > 0 && !bvs) || cap < 0 || !n_stacks_out ||
+        (cap > 0 && (!first_out || !count_out)))
+        return RF_ERR_INVALID_ARG;
+    std::vector<rf_primitive> e(n);
+    std::vector<HitRec> tab(n);
+    std::vector<float4> bs(n);
+    prepare_mixed(prims, n, e.data(), tab.data(), bs.data());
+    std::vector<char> cut(n + 1, 0);
+    for (int b = 0; b < nbv; ++b) {
+        if (bvs[b].objStartIndex >= 0 && bvs[b].objStartIndex <= n) cut[bvs[b].objStartIndex] = 1;
+        if (bvs[b].objEndIndex >= 0 && bvs[b].objEndIndex <= n) cut[bvs[b].objEndIndex] = 1;
+    }
+    mark_stacks(e.data(), n, tab.data(), bs.data(), cut);
+    int32_t k = 0;
+    for (int i = 0; i < n;) {
+        int32_t ti;
+        std::memcpy(&ti, &tab[i].aux.x, 4);
+        if (ti != kStackType) { ++i; continue; }
+        const int m = (int)tab[i].aux.y;
+        if (k < cap) {
+            first_out[k] = i;
+            count_out[k] = m;
+        }
+        ++k;
+        i += m;
+    }
+    *n_stacks_out = k;
+    return RF_OK;
+}
+
 rf_status rf_budgets_by_area(const rf_primitive *prims, int32_t n, int64_t total_rays, int64_t *rays_out)
 {
     return rf_budgets_by_density(prims, n, nullptr, total_rays, rays_out);
@@ -1725,7 +1851,8 @@ rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_sc
         cudaError_t e;
         if ((e = launch_plan_round(nrows, d_sc, d_em, d_total, d_next, c->d_seg.as<Segment>(), &bc->nseg, &bc->total, &bc->queue,
                                    kBatchChunkDraws, c->stream)) != cudaSuccess) return e;
-        if ((e = launch_batched(p, false, batch_resident(c), c->cfg.work_counts != 0, grid, c->stream)) != cudaSuccess)
+        if ((e = launch_batched(p, false, batch_resident(c), c->cfg.work_counts != 0, c->b_stacks > 0, grid,
+                                c->stream)) != cudaSuccess)
             return e;
         if ((e = launch_converge_step(c->b_hits.as<unsigned long long>(), d_total, d_off, d_len, nrows, nullptr,
                                       tol, d_next, round_rays, &bc->flags[0], c->stream)) != cudaSuccess) return e;

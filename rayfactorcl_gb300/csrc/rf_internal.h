@@ -115,11 +115,13 @@ struct LaunchCfg {
 template <class M> cudaError_t launch_trace(const LaunchCfg &cfg, const TraceParams &p, cudaStream_t st);
 template <class M> int trace_blocks_per_sm(const LaunchCfg &cfg);
 
-// Batched mixed-precision persistent kernel (rf_kern_fast.cu); count: also
-// collect the work counters (TraceParams::work).
-cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool count, int grid, cudaStream_t st);
+// Batched mixed-precision persistent kernel (rf_kern_batched.cu); count: also
+// collect the work counters (TraceParams::work); stacks: some scene's tables
+// have segment stacks (kStackType).
+cudaError_t launch_batched(const TraceParams &p, bool rec, bool resident, bool count, bool stacks, int grid,
+                           cudaStream_t st);
 // The same kernel with runBVGPU's bounding-surface semantics (one resident scene).
-cudaError_t launch_batched_bv(const TraceParams &p, bool rec, bool count, int grid, cudaStream_t st);
+cudaError_t launch_batched_bv(const TraceParams &p, bool rec, bool count, bool stacks, int grid, cudaStream_t st);
 int batched_blocks_per_sm(bool rec, bool resident);
 cudaError_t launch_build_masks(const MaskInputs &in, uint32_t *out, cudaStream_t st);
 // Mixed-precision kernel for one small scene with the plain kernel's launch shape
@@ -131,6 +133,11 @@ int mixed_small_blocks_per_sm(int gpt, bool rec);
 size_t batched_smem_bytes();
 int batched_tile();  // scenes with at most this many surfaces use the resident kernel
 constexpr int kBatchTile = 512;  // surfaces the resident kernel keeps in shared memory
+// Hit-record type of a member of a segment stack in the mixed-precision tables:
+// consecutive cylinders [a, a + m) that tile one longer cylinder, each member's
+// record holding the stack's (the first member's invm, aux = (kStackType, m,
+// util2, offset of the member in the stack as int bits)).
+constexpr int kStackType = 7;
 constexpr int kBatchBruteMax = 12;  // scenes up to this many surfaces are traced without culling
 constexpr int kEmitFrameWords = 5;  // float4 words of a planar emitter's frame (mixed kernels)
 constexpr int kBatchMaxBV = 16;     // bounding surfaces the mixed kernel takes (runBVGPU semantics)
@@ -143,9 +150,10 @@ constexpr int kBatchBlock = 1024;       // threads per block of the batched kern
 void emit_frame(const rf_primitive &e, float4 *out);
 
 // Host preparation of one scene for the batched kernel (rf_capi.cu); eps_out
-// receives the scene's self-hit threshold for the configured eps.
-void prepare_mixed_tables(const rf_primitive *prims, int n, float eps, rf_primitive *emit, HitRec *tab, float4 *bs,
-                          float *eps_out);
+// receives the scene's self-hit threshold for the configured eps; returns the
+// number of segment stacks in the tables.
+int prepare_mixed_tables(const rf_primitive *prims, int n, float eps, rf_primitive *emit, HitRec *tab, float4 *bs,
+                         float *eps_out);
 
 // FP64 post-processing and probes (rf_kern_post.cu).
 cudaError_t launch_normalise_single(const unsigned long long *hits, const int64_t *rays, int n,

@@ -120,6 +120,19 @@ __global__ void __launch_bounds__(kSmallThreads, GPT == 1 ? 4 : 1) mixed_small_k
             case RF_CYLINDER: RF_MIXED_ALL(RF_CYLINDER) break;
             case RF_FRUSTUM: RF_MIXED_ALL(RF_FRUSTUM) break;
             case RF_SPHERE: RF_MIXED_ALL(RF_SPHERE) break;
+            case kStackType: {  // one test for the segment stack j belongs to
+                const int first = stack_first(h, j);
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    bool defer = false;
+                    int ring;
+                    const float t = stack_mixed(h, ray[k], eps, defer, ring);
+                    if (t < tb[k]) { tb[k] = t; bi[k] = first + ring; }
+                    dmask |= defer ? (1u << k) : 0u;
+                }
+                j = stack_end(h, j) - 1;
+                break;
+            }
             default: break;  // validated away on the host
             }
 #undef RF_MIXED_ALL
@@ -129,7 +142,7 @@ __global__ void __launch_bounds__(kSmallThreads, GPT == 1 ? 4 : 1) mixed_small_k
         for (int k = 0; k < R; ++k) {
             const int64_t rid = (gid0 + (int64_t)(k >> 2) * blockDim.x + tid) * 4 + (k & 3);
             const bool valid = rid >= sg.ray_begin && rid < sg.ray_end;
-            const int h = valid ? resolve_brute(bi[k], (dmask >> k) & 1u, 0, n, true, s_tab, nullptr, ray[k], eps, sc,
+            const int h = valid ? resolve_brute<true>(bi[k], (dmask >> k) & 1u, 0, n, true, s_tab, nullptr, ray[k], eps, sc,
                                                 skip, nref)
                                 : -1;
             if (REC) {

@@ -103,7 +103,7 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     unsigned char *base = g_dev[dev];
 
     float seps = eps;  // eps < 0: relative to the scene's size, like rf_trace
-    prepare_mixed_tables(prims, n, eps, h_emit, h_tab, h_sph, &seps);
+    const int nstacks = prepare_mixed_tables(prims, n, eps, h_emit, h_tab, h_sph, &seps);
     for (int i = 0; i < n; ++i) emit_frame(h_emit[i], h_frame + (size_t)i * kEmitFrameWords);
     int nseg = 0;
     int64_t chunks = 0;
@@ -162,5 +162,5 @@ extern "C" rf_status rf_trace_mixed_noalloc(const rf_primitive *prims, int32_t n
     int bps = batched_blocks_per_sm(false, true);
     if (bps <= 0) bps = 1;
     const int grid = (int)(chunks < (int64_t)sms * bps ? chunks : (int64_t)sms * bps);
-    return launch_batched(p, false, true, false, grid, st) == cudaSuccess ? RF_OK : RF_ERR_CUDA;
+    return launch_batched(p, false, true, false, nstacks > 0, grid, st) == cudaSuccess ? RF_OK : RF_ERR_CUDA;
 }

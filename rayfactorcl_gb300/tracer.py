@@ -29,7 +29,7 @@ class Tracer:
     def __init__(self, precision: int = PREC_EXACT, compat: int = 0, key1: int = REF_KEY1,
                  eps: float = 1e-3, device: int = 0, block_size: int = 0, rays_per_thread: int = 0,
                  scene_id: int = 0, tally_mode: int = 0, table_mode: int = 0, test_order: int = 0,
-                 work_counts: bool = False, batched_grid: int = 0):
+                 work_counts: bool = False, batched_grid: int = 0, split_stacks: bool = False):
         L = _lib.load()
         cfg = _lib.RfConfig()
         L.rf_config_default(ctypes.byref(cfg))
@@ -46,6 +46,7 @@ class Tracer:
         cfg.test_order = test_order
         cfg.work_counts = 1 if work_counts else 0
         cfg.batched_grid = batched_grid
+        cfg.split_stacks = 1 if split_stacks else 0
         h = ctypes.c_void_p()
         check(L.rf_create(ctypes.byref(h), ctypes.byref(cfg)))
         self._h = h
@@ -278,6 +279,23 @@ def budgets_by_area(scene: Scene, total_rays: int, use_density: bool = True) -> 
     else:
         check(_lib.load().rf_budgets_by_area(ptr(prims), prims.shape[0], int(total_rays), ptr(out)))
     return out
+
+
+def segment_stacks(scene: Scene, use_bv: bool = True) -> list[tuple[int, int]]:
+    """(first surface, number of surfaces) of every segment stack the mixed
+    kernels trace as one cylinder; with use_bv, none crosses a bounding
+    surface's child range."""
+    prims = np.ascontiguousarray(scene.primitives, PRIM_DTYPE)
+    bvs = getattr(scene, "bounding_volumes", None)
+    nb = len(bvs) if (use_bv and bvs is not None) else 0
+    bv = np.ascontiguousarray(bvs, BV_DTYPE) if nb else None
+    n = prims.shape[0]
+    first = np.zeros(max(n, 1), np.int32)
+    count = np.zeros(max(n, 1), np.int32)
+    k = ctypes.c_int32()
+    check(_lib.load().rf_segment_stacks(ptr(prims), n, ptr(bv) if nb else None, nb, ptr(first), ptr(count),
+                                        first.shape[0], ctypes.byref(k)))
+    return [(int(first[i]), int(count[i])) for i in range(k.value)]
 
 
 def write_output_txt(path: str | Path, F: np.ndarray):

@@ -328,7 +328,9 @@ def test_small_scene_kernel_equals_batched(built_lib, name):
             hs, _ = t.trace(rays)
             w = t.work_counts()
         assert np.array_equal(hs, hb[0]), (name, rpt)
-        assert int(w[:6].sum()) == int(rays.sum()) * sc.n  # every ray against every surface
+        planar = np.isin(sc.primitives["type"], (3, 4, 5))
+        # every ray against every surface but a planar emitter itself
+        assert int(w[:6].sum()) == int(np.sum(rays * (sc.n - planar)))
 
 
 def test_mixed_autotune_keeps_results(built_lib):
@@ -388,3 +390,49 @@ def test_mixed_bounding_surfaces_tallies(built_lib):
     Fbar = 0.5 * (Fm + Fe)
     sig = np.sqrt(2 * np.maximum(Fbar * (1 - Fbar), 1.0 / rays[:, None]) / rays[:, None])
     assert float(np.max(np.abs(Fm - Fe) / sig)) < 5
+
+
+@pytest.mark.parametrize("name,use_bv", [("gen_furnace", True), ("gen_furnace", False), ("input-furnace", False),
+                                         ("input-W100", False)])
+def test_segment_stacks_per_ray(built_lib, oracle_lib, name, use_bv):
+    """A segment stack (consecutive cylinders tiling one longer cylinder) is one
+    cylinder test whose root names the ring: per ray it gives the ring that testing
+    the rings one by one gives (split_stacks), but for roots within rounding of the
+    rim between two rings, and it agrees with the oracles as the per-ring tests do.
+    Emitters on the stack, at its ends and off it."""
+    from rayfactorcl_gb300.tracer import segment_stacks
+    sc = golden_scene(name)
+    st = segment_stacks(sc, use_bv)
+    assert st
+    a, m = st[0]
+    emitters = sorted(set([a, a + m // 2, a + m - 1, (a + m) % sc.n, sc.n - 1]))
+    p = O.params(compat=0, use_bv=use_bv)
+    total = diff = bad = on = 0
+    with _tracer(sc, precision=PREC_MIXED) as t, _tracer(sc, precision=PREC_MIXED, split_stacks=True) as ts:
+        for e in emitters:
+            got = t.trace_rays(e, 0, 16384, use_bv=use_bv)
+            ref = ts.trace_rays(e, 0, 16384, use_bv=use_bv)
+            e64 = O.trace_rays(sc, p, e, 0, 16384, f64=True)
+            e32 = O.trace_rays(sc, p, e, 0, 16384)
+            total += got.size
+            diff += int(np.count_nonzero(got != ref))
+            bad += int(np.count_nonzero((got != e64) & (got != e32)))
+            on += int(np.count_nonzero((got >= a) & (got < a + m)))
+    assert on > total // 20
+    assert diff <= max(3, 2e-4 * total), (diff, total)
+    assert bad / total <= 2e-3, (bad, total)
+
+
+def test_segment_stacks_cut_the_tests(built_lib):
+    """On the furnace the 180 wall rings are one test instead of one per ring:
+    far fewer cylinder tests, the same tallies to within the few rim rays."""
+    sc = golden_scene("gen_furnace")
+    rays = np.full(sc.n, 40_000, np.int64)
+    res = {}
+    for split in (False, True):
+        with _tracer(sc, precision=PREC_MIXED, work_counts=True, split_stacks=split) as t:
+            hits, _ = t.trace(rays, True)
+            res[split] = (hits, t.work_counts())
+    (h0, w0), (h1, w1) = res[False], res[True]
+    assert int(w0[0]) * 4 < int(w1[0]), (w0, w1)
+    assert int(np.abs(h0 - h1).sum()) <= max(10, 2e-4 * int(rays.sum()))
