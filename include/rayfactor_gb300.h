@@ -107,9 +107,11 @@ typedef struct rf_config {
                            * rf_last_work_counts (a few per cent slower); 0 = no counting      */
     int32_t batched_grid; /* RF_PREC_MIXED: 0 = one persistent block per SM; > 0 = at most this
                            * many blocks (results do not depend on it)                         */
-    int32_t split_stacks; /* RF_PREC_MIXED: 0 = a segment stack (consecutive cylinders that tile one
-                           * longer cylinder: a furnace wall of rings) is one cylinder test whose
-                           * root's z names the ring; 1 = every ring tested on its own          */
+    int32_t split_stacks; /* RF_PREC_MIXED: 0 = a segment stack is one test -- consecutive cylinders
+                           * that tile one longer cylinder (a furnace wall of rings): one cylinder
+                           * whose root's z names the ring; consecutive concentric annuli in one
+                           * plane (an end plate of rings): one plane hit whose radius names the
+                           * ring; 1 = every ring tested on its own                              */
     uint32_t reserved;
 } rf_config;
 
@@ -194,8 +196,9 @@ rf_status rf_ray_budgets(const rf_primitive *prims, int32_t n_prims, int32_t n_s
 rf_status rf_surface_areas(const rf_primitive *prims, int32_t n_prims, double *areas_out);
 
 /* (No counterpart in the reference.)  The segment stacks RF_PREC_MIXED traces as
- * one cylinder each (rf_config.split_stacks): runs of consecutive cylinders that
- * tile one longer cylinder, never across a bounding surface's child range
+ * one test each (rf_config.split_stacks): runs of consecutive cylinders that
+ * tile one longer cylinder and of consecutive concentric annuli in one plane
+ * whose radii meet, never across a bounding surface's child range
  * (bvs may be NULL when n_bvs = 0).  Host only.  first_out / count_out get up to
  * cap stacks (first surface, number of surfaces); *n_stacks_out the number found. */
 rf_status rf_segment_stacks(const rf_primitive *prims, int32_t n_prims, const rf_bounding_volume *bvs,
@@ -295,11 +298,12 @@ rf_status rf_last_refine_count(rf_ctx *ctx, uint64_t *refined_tests);
 /* (No counterpart in the reference.)  Work of the last mixed-precision run made with
  * rf_config.work_counts = 1 (zeros otherwise): counts[0..5] ray x surface tests
  * performed by surface type (RF_CYLINDER..RF_DISC; with bounding surfaces, the
- * tests of their children: each ray also tests every bounding surface), counts[6] candidate
- * surfaces of the packets (the union of their rays' cell masks, or the surfaces
- * their bounds can reach; each then checked ray by ray), counts[7] ray packets
- * (32 rays).  Tests skipped by culling are the all-pairs count minus the sum of
- * counts[0..5]. */
+ * tests of their children: each ray also tests every bounding surface; a segment
+ * stack's one test counts once, as its members' type), counts[6] candidate
+ * surfaces the packets checked ray by ray (from the union of their rays' cell
+ * masks, or the surfaces their bounds can reach; the other members of a stack
+ * once it is tested are not checked), counts[7] ray packets (32 rays).  Tests
+ * skipped by culling are the all-pairs count minus the sum of counts[0..5]. */
 rf_status rf_last_work_counts(rf_ctx *ctx, uint64_t *counts);
 
 /* (No counterpart in the reference.)  FP32 issue-rate probe: dependent-FMA throughput of the device in FMA/s

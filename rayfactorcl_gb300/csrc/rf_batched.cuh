@@ -469,14 +469,50 @@ static __device__ __noinline__ float stack_f64(const HitRec &h, const Ray<float>
 
 // First member of the stack that surface j (a member, record h) belongs to, and
 // one past its last.
-__device__ __forceinline__ int stack_first(const HitRec &h, int j) { return j - __float_as_int(h.aux.w); }
-__device__ __forceinline__ int stack_end(const HitRec &h, int j) { return stack_first(h, j) + (int)h.aux.y; }
+__device__ __forceinline__ int stack_first(const HitRec &h, int j) { return j - (__float_as_int(h.aux.w) & 0xffff); }
+__device__ __forceinline__ int stack_count(const HitRec &h) { return (int)((unsigned)__float_as_int(h.aux.w) >> 16); }
+__device__ __forceinline__ int stack_end(const HitRec &h, int j) { return stack_first(h, j) + stack_count(h); }
+__device__ __forceinline__ bool is_stack(int type) { return type >= kStackType; }
+// The work counters' type of a test: a stack's members' own.
+__device__ __forceinline__ int stat_type(int type)
+{
+    return type == kStackType ? RF_CYLINDER : (type == kPlateType ? RF_ANNULUS : type);
+}
+
+// A plate: concentric annuli [a, a + m) in one plane and frame, each one's outer
+// squared radius (util2) the next one's inner (util1), bit for bit.  The plane is
+// hit once with annulus_hit's arithmetic; the member is the lowest whose
+// [util1, util2] holds e = |hit|^2 (a shared rim goes to the lower member, as the
+// member loop's tie rule gives), found by a binary search over the members'
+// util2 (tab: the scene's records, shared memory when resident).  The same
+// arithmetic as testing the members one by one, so the same result.
+__device__ __forceinline__ float plate_mixed(const HitRec &h, int j, const HitRec *tab, bool resident,
+                                             const Ray<float> &w, float eps, int &idx)
+{
+    const Ray<float> o = xfrm_ray<MFast>(h, w);
+    const float th = -o.sz * MFast::rcp(o.cz);
+    const float hx = o.sx + o.cx * th;
+    const float hy = o.sy + o.cy * th;
+    const float e = MFast::fma(hx, hx, hy * hy);
+    const int a = stack_first(h, j);
+    auto util2 = [&](int k) { return resident ? tab[a + k].aux.z : __ldg(&tab[a + k].aux.z); };
+    int base = 0, len = stack_count(h);  // lowest k with util2_k >= e (uniform trip count)
+    while (len > 1) {
+        const int half = len >> 1;
+        base = util2(base + half - 1) < e ? base + half : base;
+        len -= half;
+    }
+    const float lo = resident ? tab[a].aux.y : __ldg(&tab[a].aux.y);
+    idx = a + base;
+    return (e >= lo && e <= util2(base) && th > eps) ? th : MFast::inf();
+}
 
 // The mixed test of surface j (record h) -- for a stack member, the stack's --
-// with idx the surface hit (j, or the member of the stack).
+// with idx the surface hit (j, or the member of the stack); tab, resident: the
+// scene's records, for plates.
 template <bool STK>
-__device__ __forceinline__ float test_mixed(int type, const HitRec &h, int j, const Ray<float> &w, float eps, bool sc,
-                                            bool &defer, int &idx)
+__device__ __forceinline__ float test_mixed(int type, const HitRec &h, int j, const HitRec *tab, bool resident,
+                                            const Ray<float> &w, float eps, bool sc, bool &defer, int &idx)
 {
     if (STK && type == kStackType) {
         int ring;
@@ -484,6 +520,7 @@ __device__ __forceinline__ float test_mixed(int type, const HitRec &h, int j, co
         idx = stack_first(h, j) + ring;
         return t;
     }
+    if (STK && type == kPlateType) return plate_mixed(h, j, tab, resident, w, eps, idx);
     idx = j;
     return hit_mixed(type, h, w, eps, sc, defer);
 }
@@ -539,9 +576,9 @@ __device__ __forceinline__ unsigned keep_from(int k)
 // gets the surface hit; a stack's other members leave the candidate word cm and
 // the pair's second candidate (vb = 0 when jb is one): skip_to = one past the
 // stack, for later words.
-__device__ __forceinline__ float hit_hot(int type, const HitRec &h, int j, const Ray<float> &w, float eps, bool sc,
-                                         bool &defer, int &idx, int jw, unsigned &cm, int &skip_to, int jb,
-                                         unsigned &vb)
+__device__ __forceinline__ float hit_hot(int type, const HitRec &h, int j, const HitRec *tab, bool resident,
+                                         const Ray<float> &w, float eps, bool sc, bool &defer, int &idx, int jw,
+                                         unsigned &cm, int &skip_to, int jb, unsigned &vb)
 {
     switch (type) {
     case RF_RECTANGLE: return rectangle_hit<MFast>(h, w, eps);
@@ -554,6 +591,13 @@ __device__ __forceinline__ float hit_hot(int type, const HitRec &h, int j, const
         int ring;
         const float t = stack_mixed(h, w, eps, defer, ring);
         idx = stack_first(h, j) + ring;
+        skip_to = stack_end(h, j);
+        cm &= keep_from(skip_to - jw);
+        if (jb < skip_to) vb = 0u;
+        return t;
+    }
+    case kPlateType: {
+        const float t = plate_mixed(h, j, tab, resident, w, eps, idx);
         skip_to = stack_end(h, j);
         cm &= keep_from(skip_to - jw);
         if (jb < skip_to) vb = 0u;
@@ -582,13 +626,13 @@ static __device__ __noinline__ int retrace_f64(int lo, int hi, bool resident, co
         const int type = __float_as_int(h.aux.x);
         bool defer = false;
         int idx;
-        float t = test_mixed<STK>(type, h, j, ray, eps, sc, defer, idx);
+        float t = test_mixed<STK>(type, h, j, resident ? stab : gtab, resident, ray, eps, sc, defer, idx);
         if (defer) {
             t = test_f64<STK>(h, j, ray, eps, sc, idx);
             ++nf64;
         }
         if (t < tb) { tb = t; bi = idx; }
-        if (STK && type == kStackType) j = stack_end(h, j) - 1;  // one test for the whole stack
+        if (STK && is_stack(type)) j = stack_end(h, j) - 1;  // one test for the whole stack
     }
     return bi;
 }
@@ -803,10 +847,10 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                                 const int type = __float_as_int(h.aux.x);
                                 bool defer = false;
                                 int idx;
-                                const float t = test_mixed<STK>(type, h, j, ray, eps, sc, defer, idx);
+                                const float t = test_mixed<STK>(type, h, j, S.tab, true, ray, eps, sc, defer, idx);
                                 if (t < tr) { tr = t; br = idx; }
                                 dr |= defer;
-                                if (STK && type == kStackType) j = stack_end(h, j) - 1;
+                                if (STK && is_stack(type)) j = stack_end(h, j) - 1;
                             }
                             return resolve_brute<STK>(br, dr, lo, hi, true, S.tab, gtab, ray, eps, sc, skip, nref);
                         };
@@ -825,10 +869,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             const int type = __float_as_int(h.aux.x);
                             bool defer = false;
                             int idx;
-                            const float t = test_mixed<STK>(type, h, j, ray, eps, sc, defer, idx);
+                            const float t = test_mixed<STK>(type, h, j, RESIDENT ? S.tab : gtab, RESIDENT, ray, eps, sc,
+                                                            defer, idx);
                             if (t < tb) { tb = t; bi = idx; }
                             dany |= defer;
-                            if (STK && type == kStackType) j = stack_end(h, j) - 1;
+                            if (STK && is_stack(type)) j = stack_end(h, j) - 1;
                         }
                         bi = resolve_brute<STK>(bi, dany, 0, si.n, RESIDENT, S.tab, gtab, ray, eps, sc, skip, nref);
                     }
@@ -849,8 +894,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         if (j == skip) continue;
                         const HitRec h = RESIDENT ? S.tab[j] : load_rec(gtab, j);
                         const int type = __float_as_int(h.aux.x);
-                        if (STK && type == kStackType) {
-                            S.wcount[warp][RF_CYLINDER] += nv_warp;
+                        if (STK && is_stack(type)) {
+                            S.wcount[warp][type == kStackType ? RF_CYLINDER : RF_ANNULUS] += nv_warp;
                             j = stack_end(h, j) - 1;
                         } else if ((unsigned)type < 6u) {
                             S.wcount[warp][type] += nv_warp;
@@ -998,18 +1043,19 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             cm &= keep_from((STK ? skip_to : lo) - jw);  // lo, and stacks tested in an earlier word
                             if (hi < jw + 32) cm &= (1u << (hi - jw)) - 1u;
                             if (skip >= jw && skip < jw + 32) cm &= ~(1u << (skip - jw));
-                            if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
                             while (cm) {
                                 const int j = jw + __ffs(cm) - 1;
                                 cm &= cm - 1;
+                                if (COUNT && lane == 0) S.wcount[warp][6] += 1;  // candidates checked
                                 if (!__any_sync(0xffffffffu, ray_may_hit(ray, idd, S.bs[j]))) continue;
                                 const HitRec h = S.tab[j];
                                 const int type = __float_as_int(h.aux.x);
-                                if (COUNT) tcount += lane == (type == kStackType ? RF_CYLINDER : type) ? nvalid : 0;
+                                if (COUNT) tcount += lane == stat_type(type) ? nvalid : 0;
                                 bool defer = false;
                                 int idx = j;
                                 unsigned nb = 0u;
-                                const float t = STK ? hit_hot(type, h, j, ray, eps, sc, defer, idx, jw, cm, skip_to, hi, nb)
+                                const float t = STK ? hit_hot(type, h, j, S.tab, true, ray, eps, sc, defer, idx, jw, cm,
+                                                              skip_to, hi, nb)
                                                     : hit_mixed(type, h, ray, eps, sc, defer);
                                 if (t < tr) { tr = t; br = idx; }
                                 nd += defer;
@@ -1062,7 +1108,6 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             const unsigned cm0 = mcell ? __reduce_or_sync(0xffffffffu, __ldg(mcell + (jw >> 5)))
                                                        : __shfl_sync(0xffffffffu, cmask, w);  // block-uniform choice
                             unsigned cm = STK ? cm0 & keep_from(skip_to - jw) : cm0;
-                            if (COUNT && lane == 0) S.wcount[warp][6] += __popc(cm);
                             // two candidates per pass: their sphere checks are independent
                             // chains (latency hidden); tests still run in index order
                             while (cm) {  // cm is the same in every lane
@@ -1071,6 +1116,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                                 const int bb_ = cm ? __ffs(cm) - 1 : -1;
                                 cm &= cm - 1;  // 0 stays 0
                                 const int ja = jw + ba_, jb = jw + (bb_ >= 0 ? bb_ : ba_);
+                                if (COUNT && lane == 0) S.wcount[warp][6] += bb_ >= 0 ? 2 : 1;  // candidates checked
                                 const float4 sa = resident ? S.bs[ja] : __ldg(gbs + ja);
                                 const float4 sb = resident ? S.bs[jb] : __ldg(gbs + jb);
                                 const bool ma = ray_may_hit(ray, idd, sa);
@@ -1083,11 +1129,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                                     const int j = q ? jb : ja;
                                     const HitRec h = resident ? S.tab[j] : load_rec(gtab, j);
                                     const int type = __float_as_int(h.aux.x);
-                                    if (COUNT) tcount += lane == (type == kStackType ? RF_CYLINDER : type) ? nvalid : 0;
+                                    if (COUNT) tcount += lane == stat_type(type) ? nvalid : 0;
                                     bool defer = false;
                                     int idx = j;
-                                    const float t = STK ? hit_hot(type, h, j, ray, eps, sc, defer, idx, jw, cm, skip_to,
-                                                                  q ? INT_MAX : jb, vb)
+                                    const float t = STK ? hit_hot(type, h, j, resident ? S.tab : gtab, resident, ray, eps,
+                                                                  sc, defer, idx, jw, cm, skip_to, q ? INT_MAX : jb, vb)
                                                         : hit_mixed(type, h, ray, eps, sc, defer);
                                     if (t < tb) { tb = t; bi = idx; }
                                     ndef += defer;  // predicated, no branch

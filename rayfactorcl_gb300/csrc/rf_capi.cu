@@ -399,20 +399,45 @@ void prepare_mixed(const rf_primitive *prims, int n, rf_primitive *emit, HitRec 
     }
 }
 
-// Segment stacks of one scene's mixed tables (kStackType): runs of consecutive
-// cylinders [a, a + m), 2 <= m <= 65535, with the same linear part of m (axes
-// and radii), the same normal sign (util2) and each translation one axis column
-// (m's third column) past the previous one's, so that member k is the first
-// member shifted by k lengths along its axis (to 1e-6 of the transform's scale).
-// A stack never continues across an index i with cut[i] set (a bounding
-// surface's children start or end there).  Each member's record becomes the
-// stack's -- the first member's invm, aux = (kStackType, m, util2, k) -- and its
-// bounding sphere the stack's.  Returns the number of stacks.
+// Segment stacks of one scene's mixed tables, runs [a, a + m) of 2 <= m <= 65535
+// consecutive surfaces.  Cylinder stacks (kStackType): the same linear part of m
+// (axes and radii), the same normal sign (util2) and each translation one axis
+// column (m's third column) past the previous one's, so that member k is the
+// first member shifted by k lengths along its axis (to 1e-6 of the transform's
+// scale); each member's record becomes the stack's -- the first member's invm,
+// aux = (kStackType, m, util2, w).  Plates (kPlateType): annuli with bit-equal
+// transforms, each one's util2 (outer radius squared) bit-equal to the next
+// one's util1; each member keeps its record with aux = (kPlateType, util1, util2,
+// w).  w = int bits of (m << 16) | k for member k.  A stack never continues
+// across an index i with cut[i] set (a bounding surface's children start or end
+// there).  Every member's bounding sphere becomes the stack's.  Returns the
+// number of stacks.
 int mark_stacks(const rf_primitive *e, int n, HitRec *tab, float4 *bs, const std::vector<char> &cut)
 {
+    auto cont = [&](int j) { return j < n && !((size_t)j < cut.size() && cut[j]); };
     int nstacks = 0;
     for (int i = 0; i < n;) {
         int j = i + 1;
+        if (e[i].type == RF_ANNULUS) {
+            while (cont(j) && j - i < 65535 && e[j].type == RF_ANNULUS &&
+                   std::memcmp(e[j].m, e[i].m, sizeof e[i].m) == 0 &&
+                   std::memcmp(e[j].invm, e[i].invm, sizeof e[i].invm) == 0 && e[j].util1 == e[j - 1].util2 &&
+                   e[j].util1 < e[j].util2 && e[j - 1].util1 < e[j - 1].util2)
+                ++j;
+            const int m = j - i;
+            if (m >= 2) {
+                const float4 sph = object_box_sphere(e[i], std::sqrt((double)e[j - 1].util2), 0.0, 0.0);
+                for (int k = 0; k < m; ++k) {
+                    int32_t ti = kPlateType, w = (m << 16) | k;
+                    std::memcpy(&tab[i + k].aux.x, &ti, 4);
+                    std::memcpy(&tab[i + k].aux.w, &w, 4);
+                    bs[i + k] = sph;
+                }
+                ++nstacks;
+            }
+            i = j;
+            continue;
+        }
         if (e[i].type == RF_CYLINDER) {
             double scale = 0.0;  // largest column of the linear part
             for (int col = 0; col < 3; ++col) {
@@ -420,8 +445,7 @@ int mark_stacks(const rf_primitive *e, int n, HitRec *tab, float4 *bs, const std
                 for (int r = 0; r < 3; ++r) c2 += (double)e[i].m[4 * r + col] * e[i].m[4 * r + col];
                 scale = std::max(scale, std::sqrt(c2));
             }
-            while (j < n && j - i < 65535 && !((size_t)j < cut.size() && cut[j]) && e[j].type == RF_CYLINDER &&
-                   e[j].util2 == e[i].util2) {
+            while (cont(j) && j - i < 65535 && e[j].type == RF_CYLINDER && e[j].util2 == e[i].util2) {
                 bool ok = true;
                 for (int r = 0; r < 3 && ok; ++r) {
                     for (int col = 0; col < 3 && ok; ++col)
@@ -442,8 +466,8 @@ int mark_stacks(const rf_primitive *e, int n, HitRec *tab, float4 *bs, const std
             const float4 sph = object_box_sphere(e[i], 1.0, 0.0, (double)m);
             for (int k = 0; k < m; ++k) {
                 tab[i + k] = u;
-                const int32_t off = k;
-                std::memcpy(&tab[i + k].aux.w, &off, 4);
+                const int32_t w = (m << 16) | k;
+                std::memcpy(&tab[i + k].aux.w, &w, 4);
                 bs[i + k] = sph;
             }
             ++nstacks;
@@ -795,10 +819,11 @@ rf_status upload_batch(rf_ctx *c, const rf_scene_desc *scenes, int ns, bool with
         if (s == 0) {
             c->b_test_type.assign(n, 0);
             for (int i = 0; i < n; ++i) {
-                int32_t ti, k;
-                std::memcpy(&ti, &tab[i].aux.x, 4);
-                std::memcpy(&k, &tab[i].aux.w, 4);
-                c->b_test_type[i] = ti != kStackType ? ti : (k == 0 ? (int)RF_CYLINDER : -1);
+                int32_t ti, w;
+                std::memcpy(&ti, &tab[off + i].aux.x, 4);
+                std::memcpy(&w, &tab[off + i].aux.w, 4);
+                const int own = ti == kStackType ? (int)RF_CYLINDER : (ti == kPlateType ? (int)RF_ANNULUS : ti);
+                c->b_test_type[i] = (ti < kStackType || (w & 0xffff) == 0) ? own : -1;
             }
         }
         for (int i = 0; i < n; ++i) bs[off + i] = widen_sq(bs[off + i]);
@@ -1592,10 +1617,11 @@ rf_status rf_segment_stacks(const rf_primitive *prims, int32_t n, const rf_bound
     mark_stacks(e.data(), n, tab.data(), bs.data(), cut);
     int32_t k = 0;
     for (int i = 0; i < n;) {
-        int32_t ti;
+        int32_t ti, w;
         std::memcpy(&ti, &tab[i].aux.x, 4);
-        if (ti != kStackType) { ++i; continue; }
-        const int m = (int)tab[i].aux.y;
+        std::memcpy(&w, &tab[i].aux.w, 4);
+        if (ti != kStackType && ti != kPlateType) { ++i; continue; }
+        const int m = (int)((uint32_t)w >> 16);
         if (k < cap) {
             first_out[k] = i;
             count_out[k] = m;

@@ -133,11 +133,15 @@ int mixed_small_blocks_per_sm(int gpt, bool rec);
 size_t batched_smem_bytes();
 int batched_tile();  // scenes with at most this many surfaces use the resident kernel
 constexpr int kBatchTile = 512;  // surfaces the resident kernel keeps in shared memory
-// Hit-record type of a member of a segment stack in the mixed-precision tables:
-// consecutive cylinders [a, a + m) that tile one longer cylinder, each member's
-// record holding the stack's (the first member's invm, aux = (kStackType, m,
-// util2, offset of the member in the stack as int bits)).
+// Hit-record types of the members of segment stacks in the mixed-precision
+// tables.  kStackType: consecutive cylinders [a, a + m) that tile one longer
+// cylinder, each member's record holding the stack's (the first member's invm,
+// aux = (kStackType, m, util2, w)).  kPlateType: consecutive concentric annuli in
+// one plane and frame, each one's outer radius the next one's inner, each member
+// keeping its own record with aux = (kPlateType, util1, util2, w).  w = int bits
+// of (m << 16) | (offset of the member in the stack).
 constexpr int kStackType = 7;
+constexpr int kPlateType = 8;
 constexpr int kBatchBruteMax = 12;  // scenes up to this many surfaces are traced without culling
 constexpr int kEmitFrameWords = 5;  // float4 words of a planar emitter's frame (mixed kernels)
 constexpr int kBatchMaxBV = 16;     // bounding surfaces the mixed kernel takes (runBVGPU semantics)

@@ -133,6 +133,16 @@ __global__ void __launch_bounds__(kSmallThreads, GPT == 1 ? 4 : 1) mixed_small_k
                 j = stack_end(h, j) - 1;
                 break;
             }
+            case kPlateType: {  // one test for the plate j belongs to
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    int idx;
+                    const float t = plate_mixed(h, j, s_tab, true, ray[k], eps, idx);
+                    if (t < tb[k]) { tb[k] = t; bi[k] = idx; }
+                }
+                j = stack_end(h, j) - 1;
+                break;
+            }
             default: break;  // validated away on the host
             }
 #undef RF_MIXED_ALL

@@ -275,20 +275,25 @@ def test_surface_areas_and_area_budgets(built_lib):
 
 def test_segment_stacks(built_lib):
     """Runs of consecutive cylinders that tile one longer cylinder (a furnace wall
-    of rings) are found from the transforms alone; a ring moved, resized or
-    turned, or a bounding surface's child range, ends a run."""
+    of rings) and of concentric annuli in one plane whose radii meet (an end plate
+    of rings) are found from the tables alone; a ring moved, resized or turned, a
+    gap between two annuli, or a bounding surface's child range ends a run."""
     from rayfactorcl_gb300.tracer import segment_stacks
     assert segment_stacks(golden_scene("input-W100")) == [(0, 55)]
     fur = segment_stacks(golden_scene("input-furnace"))  # the reference's own furnace model
-    assert fur[:2] == [(0, 180), (180, 128)] and len(fur) == 9
+    assert fur[:2] == [(0, 180), (180, 128)] and fur[-2:] == [(360, 26), (386, 26)] and len(fur) == 11
     assert all(c >= 2 for _, c in fur)
-    for name in ("gen_mixed64", "gen_enclosure3", "gen_precision_stress", "input-C47"):
+    for name in ("gen_mixed64", "gen_enclosure3", "gen_precision_stress", "input-C47", "gen_sweep0"):
         assert segment_stacks(golden_scene(name)) == []
     sc = golden_scene("gen_furnace")
-    assert segment_stacks(sc) == [(0, 180)]
-    # a ring shifted by 1e-3 of its length, one with another radius, one turned
-    for k, edit in ((100, "shift"), (50, "radius"), (140, "turn")):
-        s2 = golden_scene("gen_furnace").__class__.from_bytes(sc.to_bytes())
+    plates = [(180, 20), (200, 20)]
+    assert segment_stacks(sc) == [(0, 180)] + plates
+
+    def edited(k, edit):
+        s2 = sc.__class__.from_bytes(sc.to_bytes())
+        if edit == "gap":
+            s2.primitives["util1"][k] *= np.float32(1.0 + 2.0 ** -20)
+            return s2
         m = s2.primitives["m"][k].astype(np.float64).reshape(3, 4)
         if edit == "shift":
             m[2, 3] += 1e-3 * m[2, 2]
@@ -297,20 +302,21 @@ def test_segment_stacks(built_lib):
         else:
             m[:, :2] = m[:, [1, 0]]  # x and y axes swapped: same cylinder, another frame
         s2.primitives["m"][k] = m.reshape(-1).astype(np.float32)
-        got = segment_stacks(s2)
-        if edit == "shift":
-            assert got == [(0, 100), (101, 79)], got
-        else:
-            assert got == [(0, k), (k + 1, 179 - k)], (edit, got)
+        return s2
+
+    assert segment_stacks(edited(100, "shift")) == [(0, 100), (101, 79)] + plates
+    for k, edit in ((50, "radius"), (140, "turn")):
+        assert segment_stacks(edited(k, edit)) == [(0, k), (k + 1, 179 - k)] + plates, edit
+    assert segment_stacks(edited(190, "gap")) == [(0, 180), (180, 10), (190, 10), (200, 20)]
     # bounding-surface child ranges cut runs
     bvs = np.array(sc.bounding_volumes, BV_DTYPE)
     cut = np.concatenate([bvs[:1], bvs])
     cut[0]["objEndIndex"] = 90
     cut[1]["objStartIndex"] = 90
-    s3 = golden_scene("gen_furnace").__class__.from_bytes(sc.to_bytes())
+    s3 = sc.__class__.from_bytes(sc.to_bytes())
     s3.bounding_volumes = cut
-    assert segment_stacks(s3) == [(0, 90), (90, 90)]
-    assert segment_stacks(s3, use_bv=False) == [(0, 180)]
+    assert segment_stacks(s3) == [(0, 90), (90, 90)] + plates
+    assert segment_stacks(s3, use_bv=False) == [(0, 180)] + plates
     L = _lib.load()
     k = ctypes.c_int32()
     assert L.rf_segment_stacks(None, 0, None, 0, None, None, 0, ctypes.byref(k)) == 1

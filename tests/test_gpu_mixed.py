@@ -424,8 +424,9 @@ def test_segment_stacks_per_ray(built_lib, oracle_lib, name, use_bv):
 
 
 def test_segment_stacks_cut_the_tests(built_lib):
-    """On the furnace the 180 wall rings are one test instead of one per ring:
-    far fewer cylinder tests, the same tallies to within the few rim rays."""
+    """On the furnace the 180 wall rings are one test instead of one per ring, and
+    so are the 20 annuli of each end plate: far fewer cylinder and annulus tests,
+    the same tallies to within the few rays on a rim between two wall rings."""
     sc = golden_scene("gen_furnace")
     rays = np.full(sc.n, 40_000, np.int64)
     res = {}
@@ -434,5 +435,5 @@ def test_segment_stacks_cut_the_tests(built_lib):
             hits, _ = t.trace(rays, True)
             res[split] = (hits, t.work_counts())
     (h0, w0), (h1, w1) = res[False], res[True]
-    assert int(w0[0]) * 4 < int(w1[0]), (w0, w1)
+    assert int(w0[0]) * 4 < int(w1[0]) and int(w0[3]) * 2 < int(w1[3]), (w0, w1)
     assert int(np.abs(h0 - h1).sum()) <= max(10, 2e-4 * int(rays.sum()))
