@@ -107,6 +107,8 @@ struct rf_ctx {
     // trace state
     DevBuf d_hits, d_seg, d_rays, d_F, d_rec, d_err, d_misc;
     PinBuf h_seg, h_rays, h_misc;
+    std::vector<Segment> seg_cache;  // the plan in d_seg when seg_valid
+    bool seg_valid = false;
     std::vector<int64_t> last_rays;
     bool have_results = false;
     int last_launches = 0;
@@ -271,6 +273,26 @@ Plan make_plan(rf_ctx *c, bool bv, bool rec)
     return pl;
 }
 
+// Put a launch's segment plan in d_seg, unless it is the plan already there (a trace
+// repeated with the same budgets): then nothing is copied and nothing waits, so the
+// host can queue the next launch while the GPU runs the previous one.  Otherwise the
+// pinned staging buffer may still feed an earlier copy: wait for the stream first.
+rf_status upload_segments(rf_ctx *c, const std::vector<Segment> &seg)
+{
+    const size_t bytes = seg.size() * sizeof(Segment);
+    if (c->seg_valid && c->seg_cache.size() == seg.size() && std::memcmp(c->seg_cache.data(), seg.data(), bytes) == 0)
+        return RF_OK;
+    c->seg_valid = false;
+    RF_CUDA(c, c->h_seg.ensure(bytes));
+    RF_CUDA(c, c->d_seg.ensure(bytes));
+    RF_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::memcpy(c->h_seg.p, seg.data(), bytes);
+    RF_CUDA(c, cudaMemcpyAsync(c->d_seg.p, c->h_seg.p, bytes, cudaMemcpyHostToDevice, c->stream));
+    c->seg_cache = seg;
+    c->seg_valid = true;
+    return RF_OK;
+}
+
 rf_status run_trace(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_chunks, Plan &pl,
                     int32_t *d_rec, int64_t rec_base, bool zero_hits)
 {
@@ -279,13 +301,7 @@ rf_status run_trace(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_ch
     c->last_launches = 0;
     c->timed = false;
     if (seg.empty() || total_chunks == 0) return RF_OK;
-    RF_CUDA(c, c->h_seg.ensure(seg.size() * sizeof(Segment)));
-    RF_CUDA(c, c->d_seg.ensure(seg.size() * sizeof(Segment)));
-    // the pinned staging buffer may still feed an earlier copy
-    RF_CUDA(c, cudaStreamSynchronize(c->stream));
-    std::memcpy(c->h_seg.p, seg.data(), seg.size() * sizeof(Segment));
-    RF_CUDA(c, cudaMemcpyAsync(c->d_seg.p, c->h_seg.p, seg.size() * sizeof(Segment),
-                               cudaMemcpyHostToDevice, c->stream));
+    if (rf_status st = upload_segments(c, seg); st != RF_OK) return st;
 
     TraceParams p{};
     p.tab = c->d_tab.as<HitRec>();
@@ -972,12 +988,7 @@ rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_
     if (zero_hits) RF_CUDA(c, cudaMemsetAsync(c->b_hits.p, 0, (size_t)c->b_hits_total * 8, c->stream));
     RF_CUDA(c, cudaMemsetAsync(c->b_counters.p, 0, sizeof(BatchCounters), c->stream));
     if (seg.empty() || total_chunks == 0) return RF_OK;
-    RF_CUDA(c, c->h_seg.ensure(seg.size() * sizeof(Segment)));
-    RF_CUDA(c, c->d_seg.ensure(seg.size() * sizeof(Segment)));
-    RF_CUDA(c, cudaStreamSynchronize(c->stream));
-    std::memcpy(c->h_seg.p, seg.data(), seg.size() * sizeof(Segment));
-    RF_CUDA(c, cudaMemcpyAsync(c->d_seg.p, c->h_seg.p, seg.size() * sizeof(Segment), cudaMemcpyHostToDevice,
-                               c->stream));
+    if (rf_status st = upload_segments(c, seg); st != RF_OK) return st;
     TraceParams p = batch_params(c);
     p.seg = c->d_seg.as<Segment>();
     p.nseg = (int32_t)seg.size();
@@ -1047,12 +1058,7 @@ rf_status run_small(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_ch
             }
         }
     }
-    RF_CUDA(c, c->h_seg.ensure(seg.size() * sizeof(Segment)));
-    RF_CUDA(c, c->d_seg.ensure(seg.size() * sizeof(Segment)));
-    RF_CUDA(c, cudaStreamSynchronize(c->stream));
-    std::memcpy(c->h_seg.p, seg.data(), seg.size() * sizeof(Segment));
-    RF_CUDA(c, cudaMemcpyAsync(c->d_seg.p, c->h_seg.p, seg.size() * sizeof(Segment), cudaMemcpyHostToDevice,
-                               c->stream));
+    if (rf_status st = upload_segments(c, seg); st != RF_OK) return st;
     TraceParams p = batch_params(c);
     p.cmask = nullptr;
     p.mask_off = nullptr;
@@ -1850,6 +1856,7 @@ rf_status rf_converge_batch(rf_ctx *c, const rf_scene_desc *scenes, int32_t n_sc
     RF_CUDA(c, c->b_rows.ensure((size_t)nrows * (8 * 3 + 4 * 3) + 64));
     int64_t *d_off = c->b_rows.as<int64_t>(), *d_total = d_off + nrows, *d_next = d_total + nrows;
     int32_t *d_len = reinterpret_cast<int32_t *>(d_next + nrows), *d_sc = d_len + nrows, *d_em = d_sc + nrows;
+    c->seg_valid = false;  // the round planner writes d_seg on the device
     RF_CUDA(c, c->d_seg.ensure((size_t)nrows * sizeof(Segment)));
     RF_CUDA(c, c->d_F.ensure((size_t)c->b_hits_total * sizeof(double)));
     RF_CUDA(c, cudaMemcpyAsync(d_off, off.data(), nrows * 8, cudaMemcpyHostToDevice, c->stream));
