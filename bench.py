@@ -124,6 +124,8 @@ WORKLOADS = {
                "cylinder; 1e9 rays spread by area (plain kernel: bounding-surface path)",
     "stress": "precision stress: thin annuli (0.999), 89.9 degree frusta, unit primitives 1e4 from the origin; "
               "1e8 rays spread by area",
+    "ref-furnace": "the reference's own furnace model (sample-geometries input-furnace.xml as its Scene loader "
+                   "reads it: 360 cylinder rings, 52 annuli, no bounding surfaces); 1e9 rays spread by area",
 }
 
 
@@ -145,6 +147,12 @@ def workload(args):
         return generators.furnace_scene()
     if args.workload == "stress":
         return generators.precision_stress()
+    if args.workload == "ref-furnace":  # tables the reference's loader wrote (tests/golden)
+        from rayfactorcl_gb300.scene import Scene
+        from rayfactorcl_gb300.tracer import budgets_by_area, surface_areas
+        sc = Scene.from_bytes((ROOT / "tests" / "golden" / "scenes" / "input-furnace.bin").read_bytes())
+        return generators.Workload("ref-furnace", "", sc, budgets_by_area(sc, 1_000_000_000, use_density=False),
+                                   surface_areas(sc))
     if args.surfaces == 64:
         return generators.mixed_scene(seed=2, total_rays=args.rays)
     frac = np.array([16, 16, 12, 10, 10], float) / 64.0

@@ -56,14 +56,19 @@ cudaError_t launch_batched_bv(const TraceParams &p, bool rec, bool count, bool s
     return stacks ? launch_b<true, true>(p, rec, true, count, grid, st) : launch_b<true, false>(p, rec, true, count, grid, st);
 }
 
+// Resident blocks per SM, queried once per process (every GPU of a run is the same
+// part): the query costs microseconds on each launch otherwise.
 template <bool REC, bool RES>
 static int occ_b()
 {
-    const size_t smem = sizeof(BatchSmem);
-    int nb = 0;
-    auto k = batched_kernel<REC, RES, false, false, false>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kBatchThreads, smem);
+    static const int nb = [] {
+        const size_t smem = sizeof(BatchSmem);
+        int r = 0;
+        auto k = batched_kernel<REC, RES, false, false, false>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k, kBatchThreads, smem) != cudaSuccess) r = 0;
+        return r;
+    }();
     return nb;
 }
 

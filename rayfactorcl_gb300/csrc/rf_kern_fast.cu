@@ -24,11 +24,17 @@ cudaError_t launch_mixed_small(const TraceParams &p, int gpt, bool rec, int grid
     return gpt == 2 ? launch_s<2, false>(p, grid, st) : launch_s<1, false>(p, grid, st);
 }
 
+// Resident blocks per SM, queried once per process (every GPU of a run is the same part).
 template <int GPT, bool REC>
 static int occ_s()
 {
-    int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mixed_small_kernel<GPT, REC>, kSmallThreads, 0);
+    static const int nb = [] {
+        int r = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, mixed_small_kernel<GPT, REC>, kSmallThreads, 0) !=
+            cudaSuccess)
+            r = 0;
+        return r;
+    }();
     return nb;
 }
 
