@@ -656,11 +656,13 @@ __device__ __forceinline__ int resolve_brute(int bi, bool deferred, int lo, int 
 // The bounding-surface walk of runBVGPU (RayFactorGPU.cl:580-619) for one ray:
 // surfaces w = 0..nbv-1 in order, each tested in mixed precision (FP64 when
 // ill-conditioned); find(lo, hi) is the ray's nearest hit among the children
-// [lo, hi) (findObject, :445-472).  It is called for every w, in every lane,
-// before the lane's own decision, so kernels whose find() is warp-wide stay in
-// step.  stale: RF_COMPAT_BV_STALE, where a plain bounding surface that becomes
-// the nearest keeps the child found under an earlier one (:596-619).
-template <class Find>
+// [lo, hi) (findObject, :445-472).  A ray needs its children's hit only when w
+// is nearer than its best so far, so find() runs only then: WARP (find() is
+// warp-wide, every lane here): when that holds in some lane of the warp, in
+// every lane, so the warp-wide steps stay in step; else per lane.  stale:
+// RF_COMPAT_BV_STALE, where a plain bounding surface that becomes the nearest
+// keeps the child found under an earlier one (:596-619).
+template <bool WARP, class Find>
 __device__ __forceinline__ int bv_select(const HitRec *bvtab, const int4 *bvinfo, int nbv, const Ray<float> &ray,
                                          float eps, bool sc, bool stale, Find find)
 {
@@ -672,8 +674,10 @@ __device__ __forceinline__ int bv_select(const HitRec *bvtab, const int4 *bvinfo
         float t = hit_mixed(__float_as_int(hb.aux.x), hb, ray, eps, sc, defer);
         if (defer) t = hit_f64(hb, ray, eps, sc);
         const int4 info = bvinfo[w];
-        const int nw = find(info.y, info.z);
-        if (t < tbest) {
+        const bool nearer = t < tbest;
+        const bool run = WARP ? __any_sync(0xffffffffu, nearer) : nearer;
+        const int nw = run ? find(info.y, info.z) : -1;  // used only when nearer
+        if (nearer) {
             if (info.x == 1) {  // test the children at once; the surface counts only if one is hit
                 obj = nw;
                 if (nw != -1) { tbest = t; bvi = w; nb = nw; }
@@ -854,7 +858,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             }
                             return resolve_brute<STK>(br, dr, lo, hi, true, S.tab, gtab, ray, eps, sc, skip, nref);
                         };
-                        bi = bv_select(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0, find);
+                        bi = bv_select<false>(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0,
+                                              find);
                     } else if (valid) {
                         float r[4];
 #pragma unroll
@@ -1078,7 +1083,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         }
                         return br;
                     };
-                    bi = bv_select(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0, find);
+                    bi = bv_select<true>(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0, find);
                 } else {
                     float tb = MFast::inf();
                     int dj = -1, ndef = 0;  // deferred FP64 tests of this lane: the last one, and how many
