@@ -437,3 +437,55 @@ def test_segment_stacks_cut_the_tests(built_lib):
     (h0, w0), (h1, w1) = res[False], res[True]
     assert int(w0[0]) * 4 < int(w1[0]) and int(w0[3]) * 2 < int(w1[3]), (w0, w1)
     assert int(np.abs(h0 - h1).sum()) <= max(10, 2e-4 * int(rays.sum()))
+
+
+def _furnace_plus(k: int):
+    """The furnace's surfaces (ring stacks and plates) followed by k surfaces of a
+    random mixed scene: past 512 surfaces the kernel reads the tables through L1."""
+    from rayfactorcl_gb300 import generators
+    from rayfactorcl_gb300.scene import Scene
+    fur = golden_scene("gen_furnace")
+    extra = generators.mixed_scene(seed=21, total_rays=4, counts=(k // 4, k // 4, k // 6, k // 6, k - 2 * (k // 4) - 2 * (k // 6))).scene
+    return Scene(primitives=np.concatenate([fur.primitives, extra.primitives]))
+
+
+def test_segment_stacks_beyond_the_shared_memory_tables(built_lib, oracle_lib):
+    """Ring stacks and plates in a 602-surface scene (tables read through L1, plate
+    radii through __ldg): per ray against ring-by-ring and the oracles."""
+    from rayfactorcl_gb300.tracer import segment_stacks
+    sc = _furnace_plus(350)
+    assert sc.n == 602 and segment_stacks(sc)[:3] == [(0, 180), (180, 20), (200, 20)]
+    p = O.params(compat=0)
+    total = diff = bad = 0
+    with _tracer(sc, precision=PREC_MIXED) as t, _tracer(sc, precision=PREC_MIXED, split_stacks=True) as ts:
+        for e in (0, 90, 185, 215, 240, 400, 601):
+            got = t.trace_rays(e, 0, 8192)
+            ref = ts.trace_rays(e, 0, 8192)
+            e64 = O.trace_rays(sc, p, e, 0, 8192, f64=True)
+            e32 = O.trace_rays(sc, p, e, 0, 8192)
+            total += got.size
+            diff += int(np.count_nonzero(got != ref))
+            bad += int(np.count_nonzero((got != e64) & (got != e32)))
+    assert diff <= max(3, 2e-4 * total), (diff, total)
+    assert bad / total <= 2e-3, (bad, total)
+
+
+def test_segment_stacks_in_batches_and_the_convergence_loop(built_lib):
+    """Scenes with stacks in a batch (any position) equal their single-scene runs, and
+    the graph-driven loop's tallies equal a batch trace with its final budgets."""
+    scenes = [golden_scene("gen_mixed64"), golden_scene("input-W100"), golden_scene("gen_furnace")]
+    rng = np.random.default_rng(5)
+    rays = [rng.integers(0, 20000, sc.n).astype(np.int64) * 4 for sc in scenes]
+    with Tracer(precision=PREC_MIXED) as t:
+        hits, _ = t.trace_batch(scenes, rays)
+    for s, (sc, r) in enumerate(zip(scenes, rays)):
+        with _tracer(sc, precision=PREC_MIXED, scene_id=s) as t1:
+            h1, _ = t1.trace(r)
+        assert np.array_equal(hits[s], h1), s
+    init = [np.full(sc.n, 4096, np.int64) for sc in scenes[1:]]
+    with Tracer(precision=PREC_MIXED) as t:
+        hc, F, final, rounds = t.converge_batch(scenes[1:], init, tol=4e-3, round_rays=8192, max_rounds=32)
+    with Tracer(precision=PREC_MIXED) as t:
+        h2, _ = t.trace_batch(scenes[1:], final)
+    for a, b in zip(hc, h2):
+        assert np.array_equal(a, b)
