@@ -1,7 +1,7 @@
 """Command line: the reference program's main() (RayFactorCL/main.cpp:275-284) on the GPU.
 
     python -m rayfactorcl_gb300 [input.xml] [-o output.txt] [--compat] [--precision exact]
-                                [--record run.json]
+                                [--record run.json] [--split-stacks]
 
 Reads the scene (Scene::readScene, Scene.cpp:24-52), runs runCL_GPURNG with
 n_samples = globalRayDensity (main.cpp:281) and writes the view-factor matrix in
@@ -33,6 +33,8 @@ def main(argv=None) -> int:
     ap.add_argument("--precision", default="exact", choices=["exact", "fast", "mixed", "fp64"])
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--record", default=None, help="write a JSON run record to this path")
+    ap.add_argument("--split-stacks", action="store_true",
+                    help="mixed precision: test every ring of a segmented wall or end plate on its own")
     args = ap.parse_args(argv)
     prec = {"exact": PREC_EXACT, "fast": PREC_FAST, "mixed": PREC_MIXED, "fp64": PREC_FP64}[args.precision]
     try:
@@ -47,7 +49,8 @@ def main(argv=None) -> int:
     try:
         rays, hits, F = run_cl_gpurng(int(scene.global_ray_density), scene, output=args.output,
                                       stats=stats, precision=prec, device=args.device,
-                                      compat=_lib.COMPAT_ALL if args.compat else 0)
+                                      compat=_lib.COMPAT_ALL if args.compat else 0,
+                                      split_stacks=args.split_stacks)
     except _lib.RfError as e:
         print(f"rayfactor_gb300: {e}", file=sys.stderr)
         return 1
