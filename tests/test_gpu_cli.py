@@ -47,7 +47,7 @@ def test_run_gpurng_mixed_follows_bounding_surfaces(built_lib):
     for split in (False, True):
         stats = {}
         rays, hits, F = run_cl_gpurng(4000, sc, output=None, stats=stats, precision=PREC_MIXED, split_stacks=split)
-        assert np.all(rays == 4000) and stats["kernel_ms"] > 0
+        assert np.all(rays == rays[0]) and rays[0] >= 4000 and stats["kernel_ms"] > 0  # whole work groups
         got.append(hits)
     assert int(np.abs(got[0] - got[1]).sum()) <= 10
     from rayfactorcl_gb300.tracer import Tracer
