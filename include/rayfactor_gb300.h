@@ -330,9 +330,9 @@ rf_status rf_measure_fp32_peak(int32_t device, double *fma_per_s);
  * tallies once the stream reaches that point.  The tallies equal those of
  * rf_trace on a context with precision RF_PREC_MIXED, scene_id 0 and the same
  * compat, key1 and eps (eps >= 0 absolute, eps < 0 relative to the scene's
- * bounding-box diagonal, as in rf_config).  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  Every call reuses the same array and clears what must start at
+ * bounding-box diagonal, as in rf_config; segment stacks as rf_config.split_stacks = 0).
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress).  Every call reuses the same array and clears what must start at
  * zero; calls whose GPU work overlaps (other streams, other host threads) race
  * on it and must be serialised by the caller.
  * ------------------------------------------------------------------------- */
