@@ -36,7 +36,11 @@
 // or that deferred more than one test, re-traces over its gated set.  Skipping
 // a surface that the ray cannot reach does not change its nearest hit; only the
 // arithmetic differs from the exact kernel.  Scenes of at most kBruteMax surfaces skip
-// steps 1-3: every thread tests its own rays against all surfaces.
+// steps 1-3: every thread tests its own rays against all surfaces.  A segment stack
+// (consecutive cylinders tiling one longer cylinder, or concentric annuli in one
+// plane) is one test wherever its first candidate member comes up; the member hit
+// is read off the root.  The scene's tables reach shared memory by bulk copies
+// (cp.async.bulk) completing on an mbarrier.
 #pragma once
 
 #include "rf_device.cuh"
