@@ -80,6 +80,7 @@ struct BatchSmem {
     float4 frame[kFrameWords];
     HitRec bvtab[kBatchMaxBV];          // bounding surfaces (runBVGPU semantics)
     int4 bvinfo[kBatchMaxBV];           // (settings, first child, end of children, 0)
+    float4 bvbs[kBatchMaxBV];           // their bounding spheres, squared widened radius in w
     int64_t chunk;
     unsigned long long bar;             // mbarrier of the bulk copies of the scene tables
     int next_packet;
@@ -660,19 +661,25 @@ __device__ __forceinline__ int resolve_brute(int bi, bool deferred, int lo, int 
 // The bounding-surface walk of runBVGPU (RayFactorGPU.cl:580-619) for one ray:
 // surfaces w = 0..nbv-1 in order, each tested in mixed precision (FP64 when
 // ill-conditioned); find(lo, hi) is the ray's nearest hit among the children
-// [lo, hi) (findObject, :445-472).  A ray needs its children's hit only when w
-// is nearer than its best so far, so find() runs only then: WARP (find() is
+// [lo, hi) (findObject, :445-472).  bvbs: the surfaces' bounding spheres.  A ray
+// needs its children's hit only when w is nearer than its best so far, so find()
+// runs only then: WARP (find() is
 // warp-wide, every lane here): when that holds in some lane of the warp, in
 // every lane, so the warp-wide steps stay in step; else per lane.  stale:
 // RF_COMPAT_BV_STALE, where a plain bounding surface that becomes the nearest
 // keeps the child found under an earlier one (:596-619).
 template <bool WARP, class Find>
-__device__ __forceinline__ int bv_select(const HitRec *bvtab, const int4 *bvinfo, int nbv, const Ray<float> &ray,
-                                         float eps, bool sc, bool stale, Find find)
+__device__ __forceinline__ int bv_select(const HitRec *bvtab, const int4 *bvinfo, const float4 *bvbs, int nbv,
+                                         const Ray<float> &ray, float eps, bool sc, bool stale, Find find)
 {
     float tbest = MFast::inf();
     int bvi = -1, obj = -1, nb = -1;  // nb: children's nearest hit of the current winner bvi
+    const float idd = MFast::rcp(ray.cx * ray.cx + ray.cy * ray.cy + ray.cz * ray.cz);
     for (int w = 0; w < nbv; ++w) {
+        // a ray that cannot reach w's bounding sphere misses w (t = inf: nothing changes);
+        // the warp skips w when that holds in every lane
+        const bool may = ray_may_hit(ray, idd, bvbs[w]);
+        if (WARP ? !__any_sync(0xffffffffu, may) : !may) continue;
         const HitRec hb = bvtab[w];
         bool defer = false;
         float t = hit_mixed(__float_as_int(hb.aux.x), hb, ray, eps, sc, defer);
@@ -792,7 +799,10 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                 if (BV) {
                     for (int i = tid; i < 4 * p.nbv; i += blockDim.x)
                         reinterpret_cast<float4 *>(S.bvtab)[i] = __ldg(reinterpret_cast<const float4 *>(p.bvtab) + i);
-                    for (int i = tid; i < p.nbv; i += blockDim.x) S.bvinfo[i] = __ldg(p.bvinfo + i);
+                    for (int i = tid; i < p.nbv; i += blockDim.x) {
+                        S.bvinfo[i] = __ldg(p.bvinfo + i);
+                        S.bvbs[i] = __ldg(p.bvsph + i);
+                    }
                 }
                 cur_scene = sg.scene;
             }
@@ -862,8 +872,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                             }
                             return resolve_brute<STK>(br, dr, lo, hi, true, S.tab, gtab, ray, eps, sc, skip, nref);
                         };
-                        bi = bv_select<false>(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0,
-                                              find);
+                        bi = bv_select<false>(S.bvtab, S.bvinfo, S.bvbs, p.nbv, ray, eps, sc,
+                                              (p.compat & RF_COMPAT_BV_STALE) != 0, find);
                     } else if (valid) {
                         float r[4];
 #pragma unroll
@@ -1087,7 +1097,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_kernel(const TracePa
                         }
                         return br;
                     };
-                    bi = bv_select<true>(S.bvtab, S.bvinfo, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0, find);
+                    bi = bv_select<true>(S.bvtab, S.bvinfo, S.bvbs, p.nbv, ray, eps, sc, (p.compat & RF_COMPAT_BV_STALE) != 0,
+                                         find);
                 } else {
                     float tb = MFast::inf();
                     int dj = -1, ndef = 0;  // deferred FP64 tests of this lane: the last one, and how many

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <limits>
 #include <map>
 #include <mutex>
 #include <new>
@@ -121,7 +122,7 @@ struct rf_ctx {
     DevBuf b_tab, b_emit, b_bsph, b_scenes, b_hits, b_rows, b_counters;
     // cell masks of the batched kernel and their inputs (built at upload)
     DevBuf b_patch, b_chain, b_plane, b_cone, b_maskrows, b_maskoff, b_mask, b_frame;
-    DevBuf b_bvtab, b_bvinfo;  // the single scene's bounding surfaces, re-centred like its surfaces
+    DevBuf b_bvtab, b_bvinfo, b_bvsph;  // the single scene's bounding surfaces, re-centred like its surfaces
     bool b_masks = false;
     double b_mask_ms = 0.0;     // device time of the last mask build
     std::vector<SceneInfo> b_info;
@@ -384,6 +385,21 @@ float4 object_box_sphere(const rf_primitive &e, double ext, double z0, double z1
     return make_float4((float)cx, (float)cy, (float)cz, (float)(rad * (1.0 + 1e-5) + 1e-6 * (cn + rad) + 1e-7));
 }
 
+// Bounding sphere of a surface (object-space box [-ext,ext]^2 x [z0,z1] by type)
+// under a re-centred record's m.
+float4 surface_sphere(const rf_primitive &e)
+{
+    double ext = 1.0, z0 = 0.0, z1 = 0.0;
+    switch (e.type) {
+    case RF_CYLINDER: z1 = 1.0; break;
+    case RF_FRUSTUM: ext = std::max(1.0, std::fabs((double)e.util1)); z1 = 1.0; break;
+    case RF_SPHERE: z0 = -1.0; z1 = 1.0; break;
+    case RF_ANNULUS: ext = std::sqrt(std::max(0.0, (double)e.util2)); break;
+    default: break;
+    }
+    return object_box_sphere(e, ext, z0, z1);
+}
+
 // Mixed-precision tables of one scene.  The world origin moves (in FP64) to the
 // mean of the surfaces' translations, so a scene placed far from the origin keeps
 // its FP32 resolution: m' = m - anchor, invm' = invm o (x + anchor).  Each surface
@@ -403,15 +419,7 @@ void prepare_mixed(const rf_primitive *prims, int n, rf_primitive *emit, HitRec 
         }
         emit[i] = e;
         tab[i] = make_hitrec(e.invm, e.type, e.util1, e.util2);
-        double ext = 1.0, z0 = 0.0, z1 = 0.0;  // object-space box [-ext,ext]^2 x [z0,z1]
-        switch (e.type) {
-        case RF_CYLINDER: z1 = 1.0; break;
-        case RF_FRUSTUM: ext = std::max(1.0, std::fabs((double)e.util1)); z1 = 1.0; break;
-        case RF_SPHERE: z0 = -1.0; z1 = 1.0; break;
-        case RF_ANNULUS: ext = std::sqrt(std::max(0.0, (double)e.util2)); break;
-        default: break;
-        }
-        bs[i] = object_box_sphere(e, ext, z0, z1);
+        bs[i] = surface_sphere(e);
     }
 }
 
@@ -1000,6 +1008,7 @@ rf_status run_batched(rf_ctx *c, const std::vector<Segment> &seg, int64_t total_
     if (bv) {
         p.bvtab = c->b_bvtab.as<HitRec>();
         p.bvinfo = c->b_bvinfo.as<int4>();
+        p.bvsph = c->b_bvsph.as<float4>();
         p.nbv = c->nbv;
         RF_CUDA(c, launch_batched_bv(p, rec, c->cfg.work_counts != 0, c->b_stacks > 0, grid, c->stream));
     } else {
@@ -1199,7 +1208,7 @@ void rf_destroy(rf_ctx *c)
                       &c->d_rays, &c->d_F, &c->d_rec, &c->d_err, &c->d_misc, &c->b_tab, &c->b_emit,
                       &c->b_bsph, &c->b_scenes, &c->b_hits, &c->b_rows, &c->b_counters, &c->b_patch,
                       &c->b_chain, &c->b_plane, &c->b_cone, &c->b_maskrows, &c->b_maskoff, &c->b_mask, &c->b_frame, &c->b_bvtab,
-                      &c->b_bvinfo})
+                      &c->b_bvinfo, &c->b_bvsph})
         b->release();
     c->h_seg.release();
     c->h_rays.release();
@@ -1284,6 +1293,7 @@ rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf
                 for (int k = 0; k < 3; ++k) a[k] += prims[i].m[4 * k + 3];
             for (int k = 0; k < 3; ++k) a[k] /= n;
             std::vector<HitRec> rb(nbv);
+            std::vector<float4> bsv(nbv);
             for (int b = 0; b < nbv; ++b) {
                 float im[12];
                 std::memcpy(im, bvs[b].invm, sizeof im);
@@ -1292,9 +1302,31 @@ rf_status rf_set_scene(rf_ctx *c, const rf_primitive *prims, int32_t n, const rf
                     im[4 * k + 3] = (float)((double)r[3] + (double)r[0] * a[0] + (double)r[1] * a[1] + (double)r[2] * a[2]);
                 }
                 rb[b] = make_hitrec(im, bvs[b].type, bvs[b].util1, bvs[b].util2);
+                // its bounding sphere: m = the inverse of the re-centred invm (FP64)
+                rf_primitive e{};
+                e.type = bvs[b].type;
+                e.util1 = bvs[b].util1;
+                e.util2 = bvs[b].util2;
+                const double A[9] = {im[0], im[1], im[2], im[4], im[5], im[6], im[8], im[9], im[10]};
+                const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                                   A[2] * (A[3] * A[7] - A[4] * A[6]);
+                const double inv[9] = {(A[4] * A[8] - A[5] * A[7]) / det, (A[2] * A[7] - A[1] * A[8]) / det,
+                                       (A[1] * A[5] - A[2] * A[4]) / det, (A[5] * A[6] - A[3] * A[8]) / det,
+                                       (A[0] * A[8] - A[2] * A[6]) / det, (A[2] * A[3] - A[0] * A[5]) / det,
+                                       (A[3] * A[7] - A[4] * A[6]) / det, (A[1] * A[6] - A[0] * A[7]) / det,
+                                       (A[0] * A[4] - A[1] * A[3]) / det};
+                for (int r = 0; r < 3; ++r) {
+                    for (int k = 0; k < 3; ++k) e.m[4 * r + k] = (float)inv[3 * r + k];
+                    e.m[4 * r + 3] = (float)-(inv[3 * r] * im[3] + inv[3 * r + 1] * im[7] + inv[3 * r + 2] * im[11]);
+                }
+                bsv[b] = std::isfinite(det) && det != 0.0 ? widen_sq(surface_sphere(e))
+                                                         : make_float4(0.f, 0.f, 0.f, std::numeric_limits<float>::infinity());
             }
             RF_CUDA(c, c->b_bvtab.ensure(sizeof(HitRec) * nbv));
             RF_CUDA(c, c->b_bvinfo.ensure(sizeof(int4) * nbv));
+            RF_CUDA(c, c->b_bvsph.ensure(sizeof(float4) * nbv));
+            RF_CUDA(c, cudaMemcpyAsync(c->b_bvsph.p, bsv.data(), sizeof(float4) * nbv, cudaMemcpyHostToDevice,
+                                       c->stream));
             RF_CUDA(c, cudaMemcpyAsync(c->b_bvtab.p, rb.data(), sizeof(HitRec) * nbv, cudaMemcpyHostToDevice, c->stream));
             RF_CUDA(c, cudaMemcpyAsync(c->b_bvinfo.p, bvinfo.data(), sizeof(int4) * nbv, cudaMemcpyHostToDevice,
                                        c->stream));

@@ -67,6 +67,7 @@ struct TraceParams {
     const float4 *frame;            // mixed kernels: per emitter kEmitFrameWords (planar emission frame)
     const uint32_t *cmask;          // batched kernel: cell masks of all rows that have them
     const int64_t *mask_off;        // per global row (prim_off + emitter): first mask word, -1 = none
+    const float4 *bvsph;            // mixed kernels: bounding sphere of each bounding surface (as bsph)
 };
 
 // Cell masks of the batched kernel (build_masks_kernel): one bit per surface for
@@ -144,7 +145,7 @@ constexpr int kStackType = 7;
 constexpr int kPlateType = 8;
 constexpr int kBatchBruteMax = 12;  // scenes up to this many surfaces are traced without culling
 constexpr int kEmitFrameWords = 5;  // float4 words of a planar emitter's frame (mixed kernels)
-constexpr int kBatchMaxBV = 16;     // bounding surfaces the mixed kernel takes (runBVGPU semantics)
+constexpr int kBatchMaxBV = 64;     // bounding surfaces the mixed kernel takes (runBVGPU semantics)
 constexpr int kBatchMaxSurfaces = 32767;  // nearest hits are kept as int16 in shared memory
 constexpr int kBatchChunkDraws = 8192;  // Philox draws per chunk of the batched kernel
 constexpr int kBatchBlock = 1024;       // threads per block of the batched kernel

@@ -315,7 +315,7 @@ def run_cl_gpurng(n_samples: int, scene: Scene, output: str | Path | None = "out
     with Tracer(**tracer_kw) as t:
         t.set_scene(scene)
         # runBVGPU when the scene asks for it (main.cpp:68-70), in every precision; the
-        # mixed kernel takes up to 16 bounding surfaces over 512 surfaces (else an error)
+        # mixed kernel takes up to 64 bounding surfaces over 512 surfaces (else an error)
         bvs = scene.bounding_volumes
         use_bv = bool(scene.use_bounding_volumes) and bvs is not None and len(bvs) > 0
         rays, hits, F = t.run_gpurng(n_samples, use_bv=use_bv)

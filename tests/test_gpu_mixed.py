@@ -260,9 +260,9 @@ def test_batch_rejects_bad_input(built_lib):
         assert ei.value.status == 2
         with pytest.raises(_lib.RfError):
             t.converge_batch([sc], [np.array([4, 4])], tol=0.0, round_rays=4, max_rounds=2)
-        # bounding-surface semantics: at most 16 bounding surfaces in the mixed kernel
+        # bounding-surface semantics: at most 64 bounding surfaces in the mixed kernel
         bv = golden_scene("input-C52-BV")
-        many = np.concatenate([bv.bounding_volumes] * 9)  # 18 > 16
+        many = np.concatenate([bv.bounding_volumes] * 33)  # 66 > 64
         t.set_scene(type(bv)(1e6, True, bv.primitives, many))
         with pytest.raises(_lib.RfError) as ei:
             t.trace([4, 4], use_bv=True)
@@ -489,3 +489,52 @@ def test_segment_stacks_in_batches_and_the_convergence_loop(built_lib):
         h2, _ = t.trace_batch(scenes[1:], final)
     for a, b in zip(hc, h2):
         assert np.array_equal(a, b)
+
+
+def _many_bounding_spheres(nbv: int):
+    """nbv copies of the 3-surface enclosure on a grid, 3 apart, each under a sphere
+    bounding surface (every other one checked immediately, settings = 1)."""
+    from rayfactorcl_gb300.scene import BV_DTYPE, Scene
+    enc = golden_scene("gen_enclosure3")
+    prims, bvs = [], np.zeros(nbv, BV_DTYPE)
+    for b in range(nbv):
+        shift = 3.0 * np.array([b % 4, (b // 4) % 4, b // 16], np.float64)
+        for pr in enc.primitives:
+            q = pr.copy()
+            m = q["m"].astype(np.float64).reshape(3, 4)
+            im = q["invm"].astype(np.float64).reshape(3, 4)
+            m[:, 3] += shift
+            im[:, 3] -= im[:, :3] @ shift
+            q["m"] = m.reshape(-1).astype(np.float32)
+            q["invm"] = im.reshape(-1).astype(np.float32)
+            prims.append(q)
+        c = shift + np.array([0.0, 0.0, 0.5])
+        r = 0.75
+        inv = np.zeros((3, 4))
+        inv[:, :3] = np.eye(3) / r
+        inv[:, 3] = -c / r
+        bvs[b]["invm"] = inv.reshape(-1).astype(np.float32)
+        bvs[b]["type"] = 2  # sphere
+        bvs[b]["settings"] = b % 2
+        bvs[b]["objStartIndex"], bvs[b]["objEndIndex"] = 3 * b, 3 * b + 3
+    return Scene(1e6, True, np.array(prims), bvs)
+
+
+@pytest.mark.parametrize("nbv", [24, 64])
+def test_mixed_many_bounding_surfaces_per_ray(built_lib, oracle_lib, nbv):
+    """Up to 64 bounding surfaces (72 and 192 surfaces): the walk skips, warp by
+    warp, the surfaces no ray of the packet can reach, and per ray it agrees with the
+    FP32 and FP64 restatements of runBVGPU as with a few."""
+    sc = _many_bounding_spheres(nbv)
+    p = O.params(compat=0, use_bv=True)
+    total = bad = hit = 0
+    with _tracer(sc, precision=PREC_MIXED) as t:
+        for e in (0, 3 * nbv // 3 + 1, 3 * nbv // 2 + 2, 3 * nbv - 1):
+            got = t.trace_rays(e, 0, 8192, use_bv=True)
+            e64 = O.trace_rays(sc, p, e, 0, 8192, f64=True)
+            e32 = O.trace_rays(sc, p, e, 0, 8192)
+            total += got.size
+            hit += int(np.count_nonzero(got >= 0))
+            bad += int(np.count_nonzero((got != e64) & (got != e32)))
+    assert hit > total // 2  # closed enclosures: rays stay in their own
+    assert bad / total <= 2e-3, (bad, total)
